@@ -1,0 +1,365 @@
+#!/usr/bin/env python
+"""Benchmark of the Coulomb streamline hot path on GB300.
+
+Workload (one step = one pass over one frame, inputs resident in HBM):
+  'topo', 1 frame: 8,000 synthetic charges (50 A cube, >= 1 A apart, none
+  within 2 A of the centre, q ~ N(0, 0.4) clipped, integer net charge),
+  100,000 seeded uniform start points in a box of half-width 1.5 A, Euler
+  step 0.001 A, at most 6,000 steps per line; per line the start-to-end
+  distance and mean curvature; a 20x20 histogram over distance [0, 5.2] and
+  curvature [0, max].  Computed in the FP32-compensated form.
+
+Printed (rank 0, one JSON line): streamlines/s (value), pair-evaluations/s,
+per-step latency p50/p99, the same workload end to end through the C ABI with
+host buffers (e2e), the roofline of the streamline kernel against the FP32
+pipe peak measured in this run, the plain FP64 form and the batched grid
+workload for comparison, the CPU baseline (the oracle's restatement of the
+reference's float arithmetic on all host cores) and the SM clocks seen.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
+Multi-GPU: one process per GPU (torchrun); each rank processes its own frame
+and lines, no data-path collective ("scaling": "weak").
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "pair-evals/s & streamlines/s, FP32-comp vs FP64 plain at stated err; p50/p99"
+N_CHARGES, N_LINES, HALF, STEP, CAP = 8000, 100_000, 1.5, 0.001, 6000
+FLOPS_PER_PAIR = 17        # 3 sub, r^2 (1 mul + 2 fma), r^-3 (2 mul), q (1 mul), 3 fma accumulate
+L2_FLUSH_BYTES = 256 << 20
+
+
+def workload_config(precision="fp32c"):
+    return {
+        "workload": "topo, 1 frame: 8,000 charges, 100,000 seeded uniform start points, half-width 1.5 A, "
+                    "step 0.001 A, cap 6,000 steps, 20x20 (distance 0-5.2 A, curvature 0-max) histogram",
+        "n_charges": N_CHARGES, "n_lines": N_LINES, "half_width_A": HALF, "step_A": STEP, "cap": CAP,
+        "histogram": [20, 20], "precision": precision,
+        "precision_detail": "FP32 pair terms, Kahan across charge tiles, TwoSum warp reduction; "
+                            "FP64 positions, box test, curvature and distance",
+        "l2": "flushed between timed steps (256 MiB device write)",
+    }
+
+
+def make_inputs(rank: int):
+    from pycpet_gb300.synth import make_frame, random_start_points
+
+    fr = make_frame(N_CHARGES, seed=1 + 1000 * rank)
+    starts = random_start_points(N_LINES, [HALF] * 3, seed=2 + 1000 * rank)
+    caps = np.full(N_LINES, CAP, dtype=np.int32)
+    return fr["x"], fr["q"], starts, caps
+
+
+def pair_evals(steps, n_charges):
+    s = np.asarray(steps, dtype=np.int64)
+    return int(np.sum(np.maximum(s, 2) + 2) * n_charges)
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        fd, self.path = tempfile.mkstemp(suffix=".csv")
+        os.close(fd)
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except OSError:
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        with open(self.path) as fh:
+            for line in fh:
+                parts = [p.strip() for p in line.split(",")]
+                if len(parts) < 9:
+                    continue
+                try:
+                    sm.append(float(parts[1]))
+                    mx.append(float(parts[2]))
+                except ValueError:
+                    continue
+                for name, v in zip(names, parts[5:9]):
+                    if v.lower() == "active":
+                        reasons.add(name)
+        os.unlink(self.path)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def cpu_baseline(x, q, starts, caps, budget_s=12.0, threads=None):
+    """The oracle's restatement of the reference's float arithmetic
+    (thread_operation, math_module.c:523-591) on all host cores, over the
+    first lines of the same workload until `budget_s` seconds have passed."""
+    from oracle import oracle
+
+    threads = threads or os.cpu_count() or 1
+    chunk = 2 * threads
+    done, t0, steps_all = 0, time.perf_counter(), []
+    while done < len(starts) and time.perf_counter() - t0 < budget_s:
+        sl = slice(done, done + chunk)
+        _, _, steps = oracle.topo_lines_f32(starts[sl], caps[sl], x, q, STEP, [HALF] * 3, threads=threads)
+        steps_all.append(steps)
+        done += len(steps)
+    dt = time.perf_counter() - t0
+    steps = np.concatenate(steps_all)
+    return {"lines": done, "seconds": dt, "streamlines_per_s": done / dt,
+            "pair_evals_per_s": pair_evals(steps, len(q)) / dt, "cores": threads}
+
+
+def run_reference(args, world):
+    """--impl reference: the reference's CPU implementation of the path (the
+    oracle's port of its float C; the reference library itself cannot be
+    built on this host) timed on the host cores, a bounded sample per step."""
+    from oracle import oracle
+
+    oracle.lib()
+    x, q, starts, caps = make_inputs(0)
+    threads = os.cpu_count() or 1
+    sample = 8 * threads
+    st, sl = starts[:sample], caps[:sample]
+    times, pe = [], 0
+    for i in range(args.warmup + args.steps):
+        t0 = time.perf_counter()
+        _, _, steps = oracle.topo_lines_f32(st, sl, x, q, STEP, [HALF] * 3, threads=threads)
+        dt = time.perf_counter() - t0
+        if i >= args.warmup:
+            times.append(dt)
+            pe = pair_evals(steps, len(q))
+    total = sum(times)
+    value = sample * len(times) / total
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": "streamlines/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * total / len(times),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (seeded; no dataset ships with the benchmark)", "config": workload_config("reference f32"),
+        "pair_evals_per_s": pe * len(times) / total,
+        "cpu_baseline": {"value": value, "unit": "streamlines/s", "cores": threads, "kind": "port",
+                         "sample": f"first {sample} of the 100,000 lines per step (same frame, starts, caps)"},
+        "e2e": {"value": value, "unit": "streamlines/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--no-extras", action="store_true", help="skip the FP64 / grid / CPU comparison legs")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        ap.error("--warmup must be >= 3")
+
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local_rank = int(os.environ.get("LOCAL_RANK", "0"))
+
+    if args.impl == "reference":
+        if rank == 0:
+            run_reference(args, world)
+        return
+
+    import torch
+    import torch.distributed as dist
+
+    torch.cuda.set_device(local_rank)
+    if world > 1:
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local_rank))
+
+    from pycpet_gb300 import build as gbuild
+    from pycpet_gb300 import _lib, topo_hist2d, topo_lines
+    from pycpet_gb300.core import GridBatch
+
+    gbuild.build_library()
+    dev = torch.device("cuda", local_rank)
+    x, q, starts, caps = make_inputs(rank)
+    d_x = torch.from_numpy(x).to(dev)
+    d_q = torch.from_numpy(q).to(dev)
+    d_starts = torch.from_numpy(starts).to(dev)
+    d_caps = torch.from_numpy(caps).to(dev)
+    flush = torch.empty(L2_FLUSH_BYTES, dtype=torch.uint8, device=dev)
+    stream = torch.cuda.current_stream(dev)
+    hist_range = ((0.0, 5.2), (0.0, None))
+
+    # step counts (deterministic) for the pair-evaluation count
+    res, steps = topo_lines(d_starts, d_caps, d_x, d_q, STEP, [HALF] * 3, precision="fp32c", return_steps=True)
+    torch.cuda.synchronize()
+    pe_step = pair_evals(steps.cpu().numpy(), N_CHARGES)
+
+    def step(ev_k0=None, ev_k1=None):
+        if ev_k0 is not None:
+            ev_k0.record(stream)
+        r = topo_lines(d_starts, d_caps, d_x, d_q, STEP, [HALF] * 3, precision="fp32c")
+        if ev_k1 is not None:
+            ev_k1.record(stream)
+        return r, topo_hist2d(r, bins=(20, 20), range=hist_range)
+
+    for _ in range(args.warmup):
+        step()
+    ffma = _lib.measure_peak(0)  # FP32 pipe peak of this GPU, measured now
+    torch.cuda.synchronize()
+
+    evs = [[torch.cuda.Event(enable_timing=True) for _ in range(4)] for _ in range(args.steps)]
+    sampler = ClockSampler(local_rank)
+    if world > 1:
+        dist.barrier()
+    torch.cuda.synchronize()
+    sampler.start()
+    for k in range(args.steps):
+        e0, ek0, ek1, e1 = evs[k]
+        e0.record(stream)
+        res, counts = step(ek0, ek1)
+        e1.record(stream)
+        flush.fill_(k & 0xFF)  # evict L2 between timed steps (outside the events)
+    torch.cuda.synchronize()
+    if world > 1:
+        dist.barrier()
+    clocks = sampler.stop()
+    _lib.check(_lib.lib().cpetgb_synchronize(stream.cuda_stream))
+    step_ms = [e[0].elapsed_time(e[3]) for e in evs]
+    kern_ms = [e[1].elapsed_time(e[2]) for e in evs]
+    total_s = sum(step_ms) * 1e-3
+    if world > 1:
+        t = torch.tensor([total_s], device=dev, dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        total_s = float(t.item())
+
+    value = N_LINES * world * args.steps / total_s
+    pe_per_s = pe_step * world * args.steps / total_s
+    avg_kern_s = statistics.mean(kern_ms) * 1e-3
+    achieved = pe_step * FLOPS_PER_PAIR / avg_kern_s
+    out = {
+        "metric": METRIC, "value": value, "unit": "streamlines/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": 1e3 * total_s / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (seeded; no dataset ships with the benchmark)",
+        "config": workload_config("fp32c"),
+        "pair_evals_per_s": pe_per_s,
+        "latency_ms": {"p50": float(np.percentile(step_ms, 50)), "p99": float(np.percentile(step_ms, 99))},
+        "roofline": {"bound": "fp32", "achieved": achieved / 1e12, "peak": ffma / 1e12, "unit": "TFLOP/s",
+                     "frac": achieved / ffma, "traffic": None,
+                     "kernel": "topo_kernel (FP32C, charges resident in shared memory)",
+                     "work": f"{FLOPS_PER_PAIR} flop per pair evaluation x sum_lines N*(max(s,2)+2)",
+                     "peak_source": "FFMA throughput measured in this run (cpetgb_measure_peak); "
+                                    "the driver's peak file has no FP32 figure"},
+        "gpu_launches": 4 * args.steps,
+        "clocks": clocks,
+    }
+
+    if rank == 0:
+        # e2e: the same step through the C ABI with host buffers in pinned memory
+        pin = lambda a: torch.from_numpy(np.ascontiguousarray(a)).pin_memory().numpy()
+        h_starts, h_caps, h_x, h_q = pin(starts), pin(caps), pin(x), pin(q)
+        topo_lines(h_starts[:1024], h_caps[:1024], h_x, h_q, STEP, [HALF] * 3, precision="fp32c")
+        e2e_t = []
+        for _ in range(max(1, min(args.steps, 3))):
+            t0 = time.perf_counter()
+            r = topo_lines(h_starts, h_caps, h_x, h_q, STEP, [HALF] * 3, precision="fp32c")
+            c = topo_hist2d(r, bins=(20, 20), range=hist_range)
+            e2e_t.append(time.perf_counter() - t0)
+        h2d = h_starts.nbytes + h_caps.nbytes + h_x.nbytes + h_q.nbytes + r.nbytes
+        d2h = r.nbytes + c.nbytes + 8 * 42
+        out["e2e"] = {"value": N_LINES / statistics.median(e2e_t), "unit": "streamlines/s",
+                      "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
+                      "path": "cpetgb_topo_lines + cpetgb_topo_hist2d, CPETGB_HOST, pinned buffers"}
+        if not args.no_extras and world == 1:
+            out.update(extras(d_starts, d_caps, d_x, d_q, torch, topo_lines, GridBatch))
+            out["cpu_baseline"] = {}
+            cb = cpu_baseline(x, q, starts, caps)
+            out["cpu_baseline"] = {"value": cb["streamlines_per_s"], "unit": "streamlines/s",
+                                   "cores": cb["cores"], "kind": "port",
+                                   "pair_evals_per_s": cb["pair_evals_per_s"],
+                                   "sample": f"first {cb['lines']} lines of the same workload "
+                                             f"({cb['seconds']:.1f} s), oracle restatement of the "
+                                             "reference's float C, all host threads"}
+        print(json.dumps(out), flush=True)
+    if world > 1:
+        dist.destroy_process_group()
+
+
+def extras(d_starts, d_caps, d_x, d_q, torch, topo_lines, GridBatch):
+    """FP64 plain form on a subset of the same lines (same subset in FP32C for
+    the speed-up), and the batched volume/ESP grid workload in both forms."""
+    from pycpet_gb300.synth import make_frame
+
+    n_sub = 16384
+    res = {}
+    for prec in ("fp32c", "fp64"):
+        topo_lines(d_starts[:n_sub], d_caps[:n_sub], d_x, d_q, STEP, [HALF] * 3, precision=prec)
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        _, steps = topo_lines(d_starts[:n_sub], d_caps[:n_sub], d_x, d_q, STEP, [HALF] * 3, precision=prec,
+                              return_steps=True)
+        e1.record()
+        torch.cuda.synchronize()
+        s = e0.elapsed_time(e1) * 1e-3
+        res[prec] = {"streamlines_per_s": n_sub / s,
+                     "pair_evals_per_s": pair_evals(steps.cpu().numpy(), N_CHARGES) / s, "seconds": s}
+    topo_cmp = {"sample": f"first {n_sub} lines", "fp32c": res["fp32c"], "fp64": res["fp64"],
+                "speedup_fp32c_vs_fp64": res["fp64"]["seconds"] / res["fp32c"]["seconds"]}
+
+    # batched volume + volume_ESP: 64 frames, N ~ U[3k, 40k], grids 11^3/21^3/31^3
+    rng = np.random.default_rng(2024)
+    frames = []
+    for f in range(64):
+        n = int(rng.integers(3000, 40001))
+        half = float(rng.choice([0.5, 1.0, 1.5]))
+        g = np.linspace(-half, half, int(round(2 * half / 0.1)) + 1)
+        pts = np.stack(np.meshgrid(g, g, g, indexing="ij"), -1).reshape(-1, 3)
+        fr = make_frame(n, seed=5000 + f)
+        frames.append((pts, fr["x"], fr["q"]))
+    grid = {}
+    for kind in ("field", "esp"):
+        for prec in ("fp32c", "fp64"):
+            gb = GridBatch(frames, kind=kind, precision=prec, device=True)
+            gb.run()
+            torch.cuda.synchronize()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            gb.run()
+            e1.record()
+            torch.cuda.synchronize()
+            s = e0.elapsed_time(e1) * 1e-3
+            grid[f"{kind}_{prec}"] = {"pair_evals_per_s": gb.pair_evals / s, "ms": s * 1e3}
+            del gb
+    grid["workload"] = "64 frames, 3,000-40,000 charges, 11^3/21^3/31^3 grids, one descriptor-table launch"
+    grid["pair_evals"] = int(sum(len(p) * len(qq) for p, _, qq in frames))
+    return {"topo_fp64_vs_fp32c": topo_cmp, "grid_batch": grid}
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,130 @@
+/*
+ * cpetgb.h -- C ABI of libcpetgb.so, the GB300 (sm_103a) implementation of
+ * PyCPET's Coulomb hot path: field / potential on point sets, streamline
+ * topology, and the topology histogram.
+ *
+ * Conventions
+ *   - Every call returns an int status: CPETGB_OK (0) or a negative code;
+ *     cpetgb_last_error() gives the message of the calling thread's last failure.
+ *   - No exceptions cross this boundary and there is no CPU fallback: without a
+ *     usable CUDA device every compute call returns CPETGB_ENODEV.
+ *   - The caller owns every buffer.  `mem` says where the data pointers live:
+ *     CPETGB_HOST (host memory; the call copies in, computes, copies out and
+ *     returns when the results are in place) or CPETGB_DEVICE (device memory of
+ *     the current device; the call is enqueued on `stream` and returns at once;
+ *     cpetgb_synchronize(stream) waits and reports errors raised on the device).
+ *   - `stream` is a cudaStream_t; NULL means the legacy default stream for
+ *     CPETGB_DEVICE calls and a library-owned stream for CPETGB_HOST calls.
+ *   - Coordinates are in Angstrom, charges in e, fields in V/A, potentials in
+ *     V; charge positions are relative to the box centre (the reference
+ *     calculator's frame after its rotation step, CPET/source/calculator.py:341-346).
+ *   - Precision: CPETGB_FP64 = every operation in IEEE double (the plain
+ *     drop-in); CPETGB_FP32C = FP32 pair terms with compensated (Kahan)
+ *     accumulation across charge tiles, FP64 for streamline positions and the
+ *     final curvature / distance.
+ */
+#ifndef CPETGB_H
+#define CPETGB_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define CPETGB_OK 0
+#define CPETGB_EINVAL (-1)   /* bad argument (size, pointer, enum) */
+#define CPETGB_ENOMEM (-2)   /* device allocation failed */
+#define CPETGB_ECUDA (-3)    /* CUDA runtime error */
+#define CPETGB_ETIMEOUT (-4) /* a bounded device-side wait gave up */
+#define CPETGB_ENODEV (-5)   /* no usable CUDA device */
+#define CPETGB_ERANGE (-6)   /* non-finite or inverted histogram range */
+
+#define CPETGB_FP64 0
+#define CPETGB_FP32C 1
+
+#define CPETGB_HOST 0
+#define CPETGB_DEVICE 1
+
+#define CPETGB_FIELD 0
+#define CPETGB_ESP 1
+
+/* ---- library ------------------------------------------------------------ */
+int cpetgb_version(void);
+/* Copies the calling thread's last error message (NUL-terminated). */
+int cpetgb_last_error(char* buf, size_t len);
+/* Number of SMs of the current device, or a negative status. */
+int cpetgb_device_sms(void);
+/* Waits for `stream` and returns (then clears) the device-side status. */
+int cpetgb_synchronize(void* stream);
+/* Precision used by the float32 drop-in entry points below (default FP32C). */
+int cpetgb_set_default_precision(int precision);
+int cpetgb_get_default_precision(void);
+
+/* Pipe throughput microbenchmark on the current device (roofline denominators):
+ * kind 0 FP32 FFMA flop/s, 1 FP64 DFMA flop/s, 2 MUFU rsqrt op/s, 3 FP32x2 FFMA2 flop/s. */
+int cpetgb_measure_peak(int kind, double* ops_per_s);
+
+/* ---- float32 drop-ins of the reference FFI (host buffers) ---------------- */
+/* compute_looped_field: CPET/utils/math_module.c:405-451, bound by
+ * CPET/utils/c_ops.py:151-159,250-263.  E[p] = k sum q (x0[p]-x)/|.|^3 with
+ * r^2 clamped at 1e-6. */
+int cpetgb_compute_looped_field(int total_points, int n_charges, const float* x_0,
+                                const float* x, const float* Q, float* E);
+/* calc_esp_base: math_module.c:453-486, c_ops.py:131-138,326-341.
+ * ESP[0] += k sum q / |x_init - x|  (accumulates, like the reference). */
+int cpetgb_calc_esp_base(float* ESP, const float* x_init, int n_charges, const float* x,
+                         const float* Q);
+/* calc_field: math_module.c:255-293, c_ops.py:113-120,360-375.  Unclamped. */
+int cpetgb_calc_field(float* E, const float* x_init, int n_charges, const float* x,
+                      const float* Q);
+/* thread_operation: math_module.c:523-591, c_ops.py:85-95,281-302.
+ * ret = {start-to-end distance, mean start/end curvature}. */
+int cpetgb_thread_operation(int n_charges, int n_iter, float step_size, const float* x_0,
+                            const float* dimensions, const float* x, const float* Q,
+                            float* ret);
+/* All lines of compute_topo_complete_c_shared (CPET/source/calculator.py:675-712)
+ * in one call: x_0[L][3], n_iter[L], ret[L][2] in start order. */
+int cpetgb_thread_operation_batch(int n_lines, int n_charges, const int32_t* n_iter,
+                                  float step_size, const float* x_0, const float* dimensions,
+                                  const float* x, const float* Q, float* ret);
+/* compute_ESP_on_grid's per-point loop (CPET/utils/calculator.py:450-475) in one
+ * call: ESP[p] = k sum q / |x_0[p] - x|. */
+int cpetgb_compute_esp_grid(int total_points, int n_charges, const float* x_0, const float* x,
+                            const float* Q, float* ESP);
+
+/* ---- general entry points (double buffers, host or device) --------------- */
+/* Field at n_points points: points[P][3], x[N][3], q[N] -> field[P][3].
+ * clamp != 0 applies compute_looped_field's r^2 >= 1e-6; clamp == 0 is calc_field. */
+int cpetgb_field_grid(int precision, int mem, int n_points, int n_charges, const double* points,
+                      const double* x, const double* q, int clamp, double* field, void* stream);
+/* Potential at n_points points (calc_esp_base per point) -> esp[P]. */
+int cpetgb_esp_grid(int precision, int mem, int n_points, int n_charges, const double* points,
+                    const double* x, const double* q, double* esp, void* stream);
+/* Many frames in one launch.  desc is a HOST array [n_frames][4] of int64:
+ * {charge_offset, n_charges, point_offset, n_points} into x/q and points/out.
+ * kind = CPETGB_FIELD (out[.][3]) or CPETGB_ESP (out[.]). */
+int cpetgb_grid_batch(int kind, int precision, int mem, int clamp, int n_frames,
+                      const int64_t* desc, const double* points, const double* x,
+                      const double* q, double* out, void* stream);
+/* Streamlines: starts[L][3], n_iter[L], half_dims (HOST, 3 half-widths).
+ * result[L][2] = {distance, mean curvature} in start order; ends[L][3] (last
+ * position) and steps[L] (Euler steps of the main loop) may be NULL. */
+int cpetgb_topo_lines(int precision, int mem, int n_lines, int n_charges, const double* starts,
+                      const int32_t* n_iter, double step, const double* half_dims,
+                      const double* x, const double* q, double* result, double* ends,
+                      int32_t* steps, void* stream);
+/* 2-D histogram of result[L][2] with numpy.histogram2d's edges and binning.
+ * range (HOST) = {dist_lo, dist_hi, curv_lo, curv_hi}; a NaN bound is taken
+ * from the data (column min / max).  counts[nb_dist][nb_curv] (uint64) are
+ * overwritten; edges (nb_dist+1 then nb_curv+1 doubles) may be NULL.
+ * nb_dist + nb_curv <= 4096. */
+int cpetgb_topo_hist2d(int mem, int n_lines, const double* result, int nb_dist, int nb_curv,
+                       const double* range, uint64_t* counts, double* edges, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* CPETGB_H */

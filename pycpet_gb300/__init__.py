@@ -1,0 +1,13 @@
+"""pycpet_gb300 -- GB300 (sm_103a) implementation of PyCPET's Coulomb hot path.
+
+Kernels live in libcpetgb.so (pycpet_gb300/csrc, C ABI in include/cpetgb.h);
+this package is the host side: ctypes binding (``_lib``), array-level API
+(``core``), and drop-ins for PyCPET's ``c_ops.Math_ops`` (``c_ops``), the
+math functions of ``CPET.utils.calculator`` (``calculator``) and the
+calculator hot-path methods (``drop_in``).
+"""
+from ._lib import CpetgbError  # noqa: F401
+from .core import (GridBatch, esp_grid, field_grid, point_field, synchronize, topo_hist2d,  # noqa: F401
+                   topo_lines)
+
+__version__ = "1.0.0"

@@ -1,0 +1,100 @@
+"""ctypes binding of libcpetgb.so (the C ABI in include/cpetgb.h).
+
+The library is loaded from the package directory, where
+``pycpet_gb300.build.build_library()`` puts it.  There is no fallback: if the
+library is missing or no CUDA device is usable, calls raise ``CpetgbError``.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+
+from .build import LIB
+
+OK = 0
+EINVAL, ENOMEM, ECUDA, ETIMEOUT, ENODEV, ERANGE = -1, -2, -3, -4, -5, -6
+FP64, FP32C = 0, 1
+HOST, DEVICE = 0, 1
+FIELD, ESP = 0, 1
+
+_CODES = {EINVAL: "EINVAL", ENOMEM: "ENOMEM", ECUDA: "ECUDA", ETIMEOUT: "ETIMEOUT",
+          ENODEV: "ENODEV", ERANGE: "ERANGE"}
+
+_lib = None
+_path = None
+
+_vp = ctypes.c_void_p
+_i = ctypes.c_int
+_d = ctypes.c_double
+_f = ctypes.c_float
+_sz = ctypes.c_size_t
+
+# name -> argument types (all return int status)
+SIGNATURES = {
+    "cpetgb_version": [],
+    "cpetgb_last_error": [ctypes.c_char_p, _sz],
+    "cpetgb_device_sms": [],
+    "cpetgb_synchronize": [_vp],
+    "cpetgb_set_default_precision": [_i],
+    "cpetgb_get_default_precision": [],
+    "cpetgb_measure_peak": [_i, ctypes.POINTER(ctypes.c_double)],
+    "cpetgb_compute_looped_field": [_i, _i, _vp, _vp, _vp, _vp],
+    "cpetgb_calc_esp_base": [_vp, _vp, _i, _vp, _vp],
+    "cpetgb_calc_field": [_vp, _vp, _i, _vp, _vp],
+    "cpetgb_thread_operation": [_i, _i, _f, _vp, _vp, _vp, _vp, _vp],
+    "cpetgb_thread_operation_batch": [_i, _i, _vp, _f, _vp, _vp, _vp, _vp, _vp],
+    "cpetgb_compute_esp_grid": [_i, _i, _vp, _vp, _vp, _vp],
+    "cpetgb_field_grid": [_i, _i, _i, _i, _vp, _vp, _vp, _i, _vp, _vp],
+    "cpetgb_esp_grid": [_i, _i, _i, _i, _vp, _vp, _vp, _vp, _vp],
+    "cpetgb_grid_batch": [_i, _i, _i, _i, _i, _vp, _vp, _vp, _vp, _vp, _vp],
+    "cpetgb_topo_lines": [_i, _i, _i, _i, _vp, _vp, _d, _vp, _vp, _vp, _vp, _vp, _vp, _vp],
+    "cpetgb_topo_hist2d": [_i, _i, _vp, _i, _i, _vp, _vp, _vp, _vp],
+}
+
+
+class CpetgbError(RuntimeError):
+    def __init__(self, code: int, msg: str):
+        super().__init__(f"cpetgb error {_CODES.get(code, code)}: {msg}")
+        self.code = code
+
+
+def lib(path: str | None = None):
+    """Load (once) and return the ctypes handle of libcpetgb.so."""
+    global _lib, _path
+    if _lib is not None and (path is None or path == _path):
+        return _lib
+    so = path or LIB
+    if not os.path.exists(so):
+        raise CpetgbError(ENODEV, f"{so} is not built (run pycpet_gb300.build.build_library())")
+    L = ctypes.CDLL(so)
+    for name, argtypes in SIGNATURES.items():
+        fn = getattr(L, name)
+        fn.argtypes = argtypes
+        fn.restype = ctypes.c_int
+    _lib, _path = L, so
+    return L
+
+
+def last_error() -> str:
+    buf = ctypes.create_string_buffer(1024)
+    lib().cpetgb_last_error(buf, len(buf))
+    return buf.value.decode(errors="replace")
+
+
+def check(rc: int) -> None:
+    if rc != OK:
+        raise CpetgbError(rc, last_error())
+
+
+def measure_peak(kind: int) -> float:
+    """Measured pipe throughput (0 FFMA flop/s, 1 DFMA flop/s, 2 MUFU op/s, 3 FFMA2 flop/s)."""
+    v = ctypes.c_double(0.0)
+    check(lib().cpetgb_measure_peak(kind, ctypes.byref(v)))
+    return v.value
+
+
+def device_sms() -> int:
+    rc = lib().cpetgb_device_sms()
+    if rc < 0:
+        check(rc)
+    return rc

@@ -1,0 +1,264 @@
+"""Array-level API over libcpetgb.so.
+
+Every function accepts either numpy arrays (host memory: the library copies in,
+computes on the GPU and copies out) or CUDA torch tensors (device memory: the
+call is enqueued on the tensor's current stream and returns device tensors;
+``synchronize()`` waits and raises device-side errors).  Torch is used only as
+a device-buffer container; all arithmetic runs in the library's kernels.
+
+Precision names: ``"fp64"`` (every operation in IEEE double, the plain form)
+and ``"fp32c"`` (FP32 pair terms with Kahan-compensated accumulation across
+charge tiles; FP64 streamline positions, curvature and distance).
+"""
+from __future__ import annotations
+
+import math
+
+import numpy as np
+
+from . import _lib
+from ._lib import DEVICE, ESP, FIELD, FP32C, FP64, HOST, check, lib
+
+PRECISIONS = {"fp64": FP64, "fp32c": FP32C, FP64: FP64, FP32C: FP32C}
+
+
+def precision_code(p) -> int:
+    try:
+        return PRECISIONS[p.lower() if isinstance(p, str) else p]
+    except KeyError:
+        raise ValueError(f"precision must be 'fp64' or 'fp32c', got {p!r}") from None
+
+
+def _is_torch(a) -> bool:
+    return type(a).__module__.split(".")[0] == "torch"
+
+
+def _host(a, dtype, shape_tail=None):
+    a = np.ascontiguousarray(a, dtype=dtype)
+    if shape_tail is not None:
+        a = a.reshape((-1,) + tuple(shape_tail))
+    return a
+
+
+def _dev(t, dtype, shape_tail=None):
+    import torch
+
+    if not (isinstance(t, torch.Tensor) and t.is_cuda):
+        raise TypeError("device calls need CUDA torch tensors for every array argument")
+    t = t.to(dtype).contiguous()
+    if shape_tail is not None:
+        t = t.reshape((-1,) + tuple(shape_tail))
+    return t
+
+
+def _stream_of(t):
+    import torch
+
+    return torch.cuda.current_stream(t.device).cuda_stream
+
+
+def synchronize(stream=None) -> None:
+    """Wait for `stream` (a torch stream, a raw handle or None for the current
+    torch stream) and raise any device-side error recorded by the kernels."""
+    if stream is None:
+        try:
+            import torch
+
+            stream = torch.cuda.current_stream().cuda_stream if torch.cuda.is_available() else 0
+        except ImportError:
+            stream = 0
+    elif hasattr(stream, "cuda_stream"):
+        stream = stream.cuda_stream
+    check(lib().cpetgb_synchronize(stream))
+
+
+# ---------------------------------------------------------------------------
+# Grids (K1 field, K2 potential)
+# ---------------------------------------------------------------------------
+
+def field_grid(points, x, q, precision="fp32c", clamp=True):
+    """E[p] = k sum_j q_j (p - x_j) / |p - x_j|^3 at every point (P,3) -> (P,3) float64.
+
+    clamp=True applies compute_looped_field's r^2 >= 1e-6 softening
+    (CPET/utils/math_module.c:431-436); clamp=False is calc_field
+    (math_module.c:255-293)."""
+    prec = precision_code(precision)
+    if _is_torch(points):
+        import torch
+
+        points, x, q = _dev(points, torch.float64, (3,)), _dev(x, torch.float64, (3,)), _dev(q, torch.float64)
+        out = torch.empty((points.shape[0], 3), dtype=torch.float64, device=points.device)
+        with torch.cuda.device(points.device):
+            check(lib().cpetgb_field_grid(prec, DEVICE, points.shape[0], q.numel(), points.data_ptr(),
+                                          x.data_ptr(), q.data_ptr(), int(bool(clamp)), out.data_ptr(),
+                                          _stream_of(points)))
+        return out
+    points, x, q = _host(points, np.float64, (3,)), _host(x, np.float64, (3,)), _host(q, np.float64)
+    out = np.empty((points.shape[0], 3))
+    check(lib().cpetgb_field_grid(prec, HOST, points.shape[0], q.size, points.ctypes.data, x.ctypes.data,
+                                  q.ctypes.data, int(bool(clamp)), out.ctypes.data, None))
+    return out
+
+
+def esp_grid(points, x, q, precision="fp32c"):
+    """phi[p] = k sum_j q_j / |p - x_j| (calc_esp_base, math_module.c:453-486) -> (P,) float64."""
+    prec = precision_code(precision)
+    if _is_torch(points):
+        import torch
+
+        points, x, q = _dev(points, torch.float64, (3,)), _dev(x, torch.float64, (3,)), _dev(q, torch.float64)
+        out = torch.empty((points.shape[0],), dtype=torch.float64, device=points.device)
+        with torch.cuda.device(points.device):
+            check(lib().cpetgb_esp_grid(prec, DEVICE, points.shape[0], q.numel(), points.data_ptr(),
+                                        x.data_ptr(), q.data_ptr(), out.data_ptr(), _stream_of(points)))
+        return out
+    points, x, q = _host(points, np.float64, (3,)), _host(x, np.float64, (3,)), _host(q, np.float64)
+    out = np.empty(points.shape[0])
+    check(lib().cpetgb_esp_grid(prec, HOST, points.shape[0], q.size, points.ctypes.data, x.ctypes.data,
+                                q.ctypes.data, out.ctypes.data, None))
+    return out
+
+
+def point_field(points, x, q, precision="fp32c"):
+    """calc_field at one or more points (unsoftened field) -> (P,3) float64."""
+    return field_grid(np.asarray(points, dtype=np.float64).reshape(-1, 3) if not _is_torch(points) else points,
+                      x, q, precision=precision, clamp=False)
+
+
+class GridBatch:
+    """Many frames evaluated in one launch through a frame descriptor table.
+
+    frames: sequence of (points (P_f,3), x (N_f,3), q (N_f,)).  The arrays are
+    concatenated once; ``run()`` may then be called repeatedly (it reuses the
+    concatenated inputs).  With ``device=True`` the inputs are uploaded once
+    into torch CUDA tensors and ``run()`` stays on the device.
+    """
+
+    def __init__(self, frames, kind="field", precision="fp32c", clamp=True, device=False):
+        self.kind = FIELD if kind == "field" else ESP
+        self.prec = precision_code(precision)
+        self.clamp = int(bool(clamp))
+        pts, xs, qs, desc = [], [], [], []
+        po = co = 0
+        for p, x, q in frames:
+            p = np.asarray(p, np.float64).reshape(-1, 3)
+            x = np.asarray(x, np.float64).reshape(-1, 3)
+            q = np.asarray(q, np.float64).reshape(-1)
+            desc.append((co, len(q), po, len(p)))
+            pts.append(p), xs.append(x), qs.append(q)
+            po += len(p)
+            co += len(q)
+        self.desc = np.ascontiguousarray(np.array(desc, dtype=np.int64).reshape(-1, 4))
+        self.points = np.ascontiguousarray(np.concatenate(pts) if pts else np.zeros((0, 3)))
+        self.x = np.ascontiguousarray(np.concatenate(xs) if xs else np.zeros((0, 3)))
+        self.q = np.ascontiguousarray(np.concatenate(qs) if qs else np.zeros(0))
+        self.n_points = po
+        self.n_charges = co
+        self.nc = 3 if self.kind == FIELD else 1
+        self.device = device
+        if device:
+            import torch
+
+            self.points = torch.from_numpy(self.points).cuda()
+            self.x = torch.from_numpy(self.x).cuda()
+            self.q = torch.from_numpy(self.q).cuda()
+            self.out = torch.empty((po, self.nc), dtype=torch.float64, device=self.points.device)
+
+    @property
+    def pair_evals(self) -> int:
+        return int(np.sum(self.desc[:, 1] * self.desc[:, 3]))
+
+    def run(self, out=None):
+        if self.device:
+            out = self.out if out is None else out
+            with __import__("torch").cuda.device(self.points.device):
+                check(lib().cpetgb_grid_batch(self.kind, self.prec, DEVICE, self.clamp, len(self.desc),
+                                              self.desc.ctypes.data, self.points.data_ptr(), self.x.data_ptr(),
+                                              self.q.data_ptr(), out.data_ptr(), _stream_of(self.points)))
+            return out
+        out = np.empty((self.n_points, self.nc)) if out is None else out
+        check(lib().cpetgb_grid_batch(self.kind, self.prec, HOST, self.clamp, len(self.desc), self.desc.ctypes.data,
+                                      self.points.ctypes.data, self.x.ctypes.data, self.q.ctypes.data,
+                                      out.ctypes.data, None))
+        return out
+
+    def split(self, out):
+        """Per-frame views of a run() output."""
+        return [out[po:po + P] for _, _, po, P in self.desc]
+
+
+# ---------------------------------------------------------------------------
+# Streamlines (K3) and histogram (K4)
+# ---------------------------------------------------------------------------
+
+def topo_lines(starts, n_iter, x, q, step, half_dims, precision="fp32c", return_ends=False,
+               return_steps=False):
+    """thread_operation (CPET/utils/math_module.c:523-591) for every start point.
+
+    Returns result (L,2) = [distance, mean curvature] in start order, and
+    optionally the end points (L,3) and the Euler step counts (L,)."""
+    prec = precision_code(precision)
+    half = np.ascontiguousarray(np.asarray(half_dims, dtype=np.float64).reshape(3))
+    if _is_torch(starts):
+        import torch
+
+        starts, x, q = _dev(starts, torch.float64, (3,)), _dev(x, torch.float64, (3,)), _dev(q, torch.float64)
+        L = starts.shape[0]
+        n_iter = _dev(n_iter if _is_torch(n_iter) else torch.as_tensor(np.broadcast_to(n_iter, (L,)).copy(),
+                                                                       device=starts.device),
+                      torch.int32)
+        dev = starts.device
+        res = torch.empty((L, 2), dtype=torch.float64, device=dev)
+        ends = torch.empty((L, 3), dtype=torch.float64, device=dev) if return_ends else None
+        steps = torch.empty((L,), dtype=torch.int32, device=dev) if return_steps else None
+        with torch.cuda.device(dev):
+            check(lib().cpetgb_topo_lines(prec, DEVICE, L, q.numel(), starts.data_ptr(), n_iter.data_ptr(),
+                                          float(step), half.ctypes.data, x.data_ptr(), q.data_ptr(),
+                                          res.data_ptr(), ends.data_ptr() if ends is not None else None,
+                                          steps.data_ptr() if steps is not None else None, _stream_of(starts)))
+    else:
+        starts = _host(starts, np.float64, (3,))
+        L = starts.shape[0]
+        n_iter = np.ascontiguousarray(np.broadcast_to(np.asarray(n_iter), (L,)), dtype=np.int32)
+        x, q = _host(x, np.float64, (3,)), _host(q, np.float64)
+        res = np.empty((L, 2))
+        ends = np.empty((L, 3)) if return_ends else None
+        steps = np.empty(L, dtype=np.int32) if return_steps else None
+        check(lib().cpetgb_topo_lines(prec, HOST, L, q.size, starts.ctypes.data, n_iter.ctypes.data, float(step),
+                                      half.ctypes.data, x.ctypes.data, q.ctypes.data, res.ctypes.data,
+                                      ends.ctypes.data if ends is not None else None,
+                                      steps.ctypes.data if steps is not None else None, None))
+    out = [res]
+    if return_ends:
+        out.append(ends)
+    if return_steps:
+        out.append(steps)
+    return out[0] if len(out) == 1 else tuple(out)
+
+
+def topo_hist2d(result, bins=(20, 20), range=((0.0, 5.2), (0.0, None)), return_edges=False):
+    """2-D histogram of (distance, curvature) rows with numpy.histogram2d's
+    edges and binning (CPET/utils/calculator.py:702-707).  A range bound of
+    None is taken from the data (column min or max).  Returns int64 counts of
+    shape bins (and the two edge arrays)."""
+    nb0, nb1 = (int(bins), int(bins)) if np.isscalar(bins) else (int(bins[0]), int(bins[1]))
+    rng = np.array([math.nan if v is None else float(v) for pair in range for v in pair], dtype=np.float64)
+    if _is_torch(result):
+        import torch
+
+        result = _dev(result, torch.float64, (2,))
+        counts = torch.empty((nb0, nb1), dtype=torch.int64, device=result.device)
+        edges = torch.empty((nb0 + nb1 + 2,), dtype=torch.float64, device=result.device)
+        with torch.cuda.device(result.device):
+            check(lib().cpetgb_topo_hist2d(DEVICE, result.shape[0], result.data_ptr(), nb0, nb1, rng.ctypes.data,
+                                           counts.data_ptr(), edges.data_ptr(), _stream_of(result)))
+    else:
+        result = _host(result, np.float64, (2,))
+        counts = np.empty((nb0, nb1), dtype=np.uint64)
+        edges = np.empty(nb0 + nb1 + 2)
+        check(lib().cpetgb_topo_hist2d(HOST, result.shape[0], result.ctypes.data, nb0, nb1, rng.ctypes.data,
+                                       counts.ctypes.data, edges.ctypes.data, None))
+        counts = counts.astype(np.int64)
+    if return_edges:
+        return counts, edges[:nb0 + 1], edges[nb0 + 1:]
+    return counts

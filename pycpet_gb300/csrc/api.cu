@@ -1,0 +1,536 @@
+// api.cu -- the C ABI of libcpetgb.so (declared in include/cpetgb.h).
+//
+// Host-side responsibilities: argument validation, the per-device context
+// (SM count, a library stream for host-memory calls, the device status word),
+// stream-ordered scratch memory (cudaMallocAsync on the call's stream),
+// host<->device staging for CPETGB_HOST calls, the work decomposition of the
+// grid kernels (point tiles x charge splits, largest first), and the mapping
+// of device-side status words to return codes.
+#include <algorithm>
+#include <atomic>
+#include <climits>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "cpetgb.h"
+#include "kernels.cuh"
+
+using namespace cpetgb;
+
+namespace {
+
+constexpr int kVersion = 10000;  // 1.0.0
+constexpr int kMaxDevices = 64;
+
+thread_local std::string g_err;
+std::mutex g_mu;
+std::atomic<int> g_default_prec{CPETGB_FP32C};
+
+struct Ctx {
+  bool ready = false;
+  int sms = 0;
+  cudaStream_t stream = nullptr;  // used by CPETGB_HOST calls without a stream
+  int* status = nullptr;          // device status word (DevStatus)
+};
+Ctx g_ctx[kMaxDevices];
+
+int fail(int code, const char* fmt, ...) {
+  char buf[512];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof buf, fmt, ap);
+  va_end(ap);
+  g_err = buf;
+  return code;
+}
+
+int cuda_fail(cudaError_t e, const char* what) {
+  cudaGetLastError();  // clear a sticky launch error of this thread
+  const int code = (e == cudaErrorMemoryAllocation) ? CPETGB_ENOMEM : CPETGB_ECUDA;
+  return fail(code, "%s: %s", what, cudaGetErrorString(e));
+}
+
+#define CK(expr, what)                          \
+  do {                                          \
+    cudaError_t e_ = (expr);                    \
+    if (e_ != cudaSuccess) return cuda_fail(e_, what); \
+  } while (0)
+
+Ctx* context(int* rc) {
+  int dev = -1, count = 0;
+  if (cudaGetDeviceCount(&count) != cudaSuccess || count <= 0) {
+    cudaGetLastError();
+    *rc = fail(CPETGB_ENODEV, "no CUDA device available");
+    return nullptr;
+  }
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices) {
+    cudaGetLastError();
+    *rc = fail(CPETGB_ENODEV, "cannot query the current CUDA device");
+    return nullptr;
+  }
+  Ctx& c = g_ctx[dev];
+  std::lock_guard<std::mutex> lock(g_mu);
+  if (!c.ready) {
+    cudaError_t e = cudaDeviceGetAttribute(&c.sms, cudaDevAttrMultiProcessorCount, dev);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c.stream, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaMalloc(&c.status, sizeof(int));
+    if (e == cudaSuccess) e = cudaMemset(c.status, 0, sizeof(int));
+    if (e == cudaSuccess) {
+      // Keep freed scratch in the device's stream-ordered pool.
+      cudaMemPool_t pool;
+      if (cudaDeviceGetDefaultMemPool(&pool, dev) == cudaSuccess) {
+        uint64_t keep = UINT64_MAX;
+        cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep);
+      }
+    }
+    if (e != cudaSuccess) {
+      *rc = cuda_fail(e, "device context setup");
+      return nullptr;
+    }
+    c.ready = true;
+  }
+  *rc = CPETGB_OK;
+  return &c;
+}
+
+// Stream-ordered scratch, released (to the pool) on the same stream.
+struct Scratch {
+  cudaStream_t s;
+  std::vector<void*> ptrs;
+  explicit Scratch(cudaStream_t st) : s(st) {}
+  ~Scratch() {
+    for (void* p : ptrs) cudaFreeAsync(p, s);
+  }
+  template <typename T>
+  cudaError_t get(T** p, size_t count) {
+    *p = nullptr;
+    if (count == 0) count = 1;
+    void* v = nullptr;
+    cudaError_t e = cudaMallocAsync(&v, ((count * sizeof(T) + 255) / 256) * 256, s);
+    if (e == cudaSuccess) {
+      ptrs.push_back(v);
+      *p = static_cast<T*>(v);
+    }
+    return e;
+  }
+};
+
+template <typename T>
+cudaError_t h2d(T** dst, Scratch& S, const T* src, size_t count) {
+  cudaError_t e = S.get(dst, count);
+  if (e == cudaSuccess && count)
+    e = cudaMemcpyAsync(*dst, src, count * sizeof(T), cudaMemcpyHostToDevice, S.s);
+  return e;
+}
+
+// Waits for the stream and converts the device status word into a return code.
+int finish(Ctx* c, cudaStream_t s) {
+  CK(cudaStreamSynchronize(s), "stream synchronize");
+  int st = 0;
+  CK(cudaMemcpy(&st, c->status, sizeof(int), cudaMemcpyDeviceToHost), "status read");
+  if (st != kDevOk) {
+    cudaMemset(c->status, 0, sizeof(int));
+    if (st == kDevWaitTimeout)
+      return fail(CPETGB_ETIMEOUT, "a device-side wait exceeded its limit");
+    if (st == kDevBadArgument)
+      return fail(CPETGB_ERANGE, "histogram range is not finite or is inverted");
+    if (st == kDevBadCap)
+      return fail(CPETGB_EINVAL, "a streamline step cap exceeds %d", kMaxLineCap);
+    return fail(CPETGB_ECUDA, "device status %d", st);
+  }
+  return CPETGB_OK;
+}
+
+bool valid_prec(int p) { return p == CPETGB_FP64 || p == CPETGB_FP32C; }
+bool valid_mem(int m) { return m == CPETGB_HOST || m == CPETGB_DEVICE; }
+size_t packed_size(int prec) { return prec == CPETGB_FP32C ? 16 : 32; }
+
+// ---------------------------------------------------------------------------
+// Grid work decomposition.
+// ---------------------------------------------------------------------------
+struct GridPlan {
+  std::vector<GridItem> items;
+  std::vector<GridFinal> finals;
+  int n_slots = 0;
+};
+
+void plan_grid(int n_frames, const int64_t* desc, int sms, GridPlan& plan) {
+  double total = 0.0;
+  for (int f = 0; f < n_frames; ++f) total += double(desc[4 * f + 1]) * double(desc[4 * f + 3]);
+  // Aim for about 8 items per SM so the largest-first order balances the tail.
+  const double target = std::max(1.0, total / (double(std::max(sms, 1)) * 8.0));
+  for (int f = 0; f < n_frames; ++f) {
+    const int64_t co = desc[4 * f + 0], n = desc[4 * f + 1];
+    const int64_t po = desc[4 * f + 2], P = desc[4 * f + 3];
+    for (int64_t pb = 0; pb < P; pb += kGridTilePts) {
+      const int pc = static_cast<int>(std::min<int64_t>(kGridTilePts, P - pb));
+      int64_t split = 1;
+      if (n > 0) {
+        const double cost = double(pc) * double(n);
+        split = static_cast<int64_t>(std::ceil(cost / target));
+        split = std::max<int64_t>(1, std::min<int64_t>(split, std::max<int64_t>(1, n / 256)));
+      }
+      const int64_t chunk = n > 0 ? (n + split - 1) / split : 0;
+      if (n > 0) split = (n + chunk - 1) / chunk;
+      int slot_base = -1;
+      if (split > 1) {
+        slot_base = plan.n_slots;
+        plan.n_slots += static_cast<int>(split);
+        plan.finals.push_back(GridFinal{po + pb, pc, slot_base, static_cast<int32_t>(split), 0});
+      }
+      for (int64_t k = 0; k < split; ++k) {
+        GridItem it;
+        it.charge_off = co;
+        it.point_off = po;
+        it.p_begin = static_cast<int32_t>(pb);
+        it.p_count = pc;
+        it.n_begin = static_cast<int32_t>(k * chunk);
+        it.n_count = static_cast<int32_t>(std::min<int64_t>(chunk, n - k * chunk));
+        it.slot = split > 1 ? slot_base + static_cast<int32_t>(k) : -1;
+        it.pad = 0;
+        plan.items.push_back(it);
+      }
+    }
+  }
+  std::stable_sort(plan.items.begin(), plan.items.end(), [](const GridItem& a, const GridItem& b) {
+    return int64_t(a.p_count) * a.n_count > int64_t(b.p_count) * b.n_count;
+  });
+}
+
+int grid_batch_impl(int kind, int prec, int mem, int clamp, int n_frames, const int64_t* desc,
+                    const double* pts, const double* x, const double* q, double* out,
+                    void* stream) {
+  if (kind != CPETGB_FIELD && kind != CPETGB_ESP) return fail(CPETGB_EINVAL, "bad grid kind %d", kind);
+  if (!valid_prec(prec)) return fail(CPETGB_EINVAL, "bad precision %d", prec);
+  if (!valid_mem(mem)) return fail(CPETGB_EINVAL, "bad memory kind %d", mem);
+  if (n_frames < 0 || (n_frames > 0 && !desc)) return fail(CPETGB_EINVAL, "bad frame table");
+  int64_t tot_pts = 0, tot_ch = 0;
+  for (int f = 0; f < n_frames; ++f) {
+    const int64_t co = desc[4 * f], n = desc[4 * f + 1], po = desc[4 * f + 2], P = desc[4 * f + 3];
+    if (co < 0 || n < 0 || po < 0 || P < 0 || n > INT_MAX || P > INT_MAX)
+      return fail(CPETGB_EINVAL, "frame %d: negative or oversized offset/count", f);
+    tot_pts = std::max(tot_pts, po + P);
+    tot_ch = std::max(tot_ch, co + n);
+  }
+  if (tot_pts == 0) return CPETGB_OK;
+  if (!pts || !out) return fail(CPETGB_EINVAL, "points/output pointer is NULL");
+  if (tot_ch > 0 && (!x || !q)) return fail(CPETGB_EINVAL, "charge pointer is NULL");
+  int rc;
+  Ctx* c = context(&rc);
+  if (!c) return rc;
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  if (mem == CPETGB_HOST && !s) s = c->stream;
+  const int NC = kind == CPETGB_FIELD ? 3 : 1;
+
+  GridPlan plan;
+  plan_grid(n_frames, desc, c->sms, plan);
+
+  Scratch S(s);
+  const double *dp = pts, *dx = x, *dq = q;
+  double* dout = out;
+  if (mem == CPETGB_HOST) {
+    CK(h2d(const_cast<double**>(&dp), S, pts, size_t(tot_pts) * 3), "copy points");
+    if (tot_ch) {
+      CK(h2d(const_cast<double**>(&dx), S, x, size_t(tot_ch) * 3), "copy charge positions");
+      CK(h2d(const_cast<double**>(&dq), S, q, size_t(tot_ch)), "copy charges");
+    }
+    CK(S.get(&dout, size_t(tot_pts) * NC), "alloc output");
+  }
+  unsigned char* packed = nullptr;
+  GridItem* d_items = nullptr;
+  GridFinal* d_fin = nullptr;
+  double* partial = nullptr;
+  CK(S.get(&packed, size_t(std::max<int64_t>(tot_ch, 1)) * packed_size(prec)), "alloc packed charges");
+  CK(h2d(&d_items, S, plan.items.data(), plan.items.size()), "copy work items");
+  if (!plan.finals.empty()) {
+    CK(h2d(&d_fin, S, plan.finals.data(), plan.finals.size()), "copy split table");
+    CK(S.get(&partial, size_t(plan.n_slots) * kGridTilePts * 3), "alloc partial sums");
+  }
+  if (reinterpret_cast<uintptr_t>(packed) % 16 != 0)  // bulk async copies need 16-byte sources
+    return fail(CPETGB_ECUDA, "scratch allocation is not 16-byte aligned");
+  CK(launch_pack_charges(prec, tot_ch, tot_ch, dx, dq, packed, s), "pack charges");
+  CK(launch_grid(prec, kind, clamp ? 1 : 0, static_cast<int>(plan.items.size()), d_items, packed,
+                 dp, dout, partial, c->status, s),
+     "grid kernel launch");
+  CK(launch_grid_final(kind, static_cast<int>(plan.finals.size()), d_fin, partial, dout, s),
+     "grid reduction launch");
+  if (mem == CPETGB_HOST) {
+    CK(cudaMemcpyAsync(out, dout, size_t(tot_pts) * NC * sizeof(double), cudaMemcpyDeviceToHost, s),
+       "copy output");
+    return finish(c, s);
+  }
+  return CPETGB_OK;
+}
+
+int topo_impl(int prec, int mem, int L, int N, const double* starts, const int32_t* n_iter,
+              double step, const double* half, const double* x, const double* q, double* result,
+              double* ends, int32_t* steps, void* stream) {
+  if (!valid_prec(prec)) return fail(CPETGB_EINVAL, "bad precision %d", prec);
+  if (!valid_mem(mem)) return fail(CPETGB_EINVAL, "bad memory kind %d", mem);
+  if (L < 0 || N < 0) return fail(CPETGB_EINVAL, "negative line or charge count");
+  if (!half) return fail(CPETGB_EINVAL, "half_dims is NULL");
+  for (int k = 0; k < 3; ++k)
+    if (!std::isfinite(half[k]) || half[k] < 0)
+      return fail(CPETGB_EINVAL, "half_dims[%d] must be finite and >= 0", k);
+  if (!std::isfinite(step)) return fail(CPETGB_EINVAL, "step must be finite");
+  if (L == 0) return CPETGB_OK;
+  if (!starts || !n_iter || !result) return fail(CPETGB_EINVAL, "line pointer is NULL");
+  if (N > 0 && (!x || !q)) return fail(CPETGB_EINVAL, "charge pointer is NULL");
+  int rc;
+  Ctx* c = context(&rc);
+  if (!c) return rc;
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  if (mem == CPETGB_HOST && !s) s = c->stream;
+
+  Scratch S(s);
+  const double *ds = starts, *dx = x, *dq = q;
+  const int32_t* dn = n_iter;
+  double *dres = result, *dends = ends;
+  int32_t* dsteps = steps;
+  if (mem == CPETGB_HOST) {
+    CK(h2d(const_cast<double**>(&ds), S, starts, size_t(L) * 3), "copy starts");
+    CK(h2d(const_cast<int32_t**>(&dn), S, n_iter, size_t(L)), "copy n_iter");
+    if (N) {
+      CK(h2d(const_cast<double**>(&dx), S, x, size_t(N) * 3), "copy charge positions");
+      CK(h2d(const_cast<double**>(&dq), S, q, size_t(N)), "copy charges");
+    }
+    CK(S.get(&dres, size_t(L) * 2), "alloc result");
+    if (ends) CK(S.get(&dends, size_t(L) * 3), "alloc ends");
+    if (steps) CK(S.get(&dsteps, size_t(L)), "alloc steps");
+  }
+  const int pad = topo_charge_pad();
+  const int64_t n_pad = ((std::max(N, 1) + int64_t(pad) - 1) / pad) * pad;
+  unsigned char* packed = nullptr;
+  int* queue = nullptr;
+  CK(S.get(&packed, size_t(n_pad) * packed_size(prec)), "alloc packed charges");
+  CK(S.get(&queue, 1), "alloc queue");
+  CK(cudaMemsetAsync(queue, 0, sizeof(int), s), "zero queue");
+  if (reinterpret_cast<uintptr_t>(packed) % 16 != 0)
+    return fail(CPETGB_ECUDA, "scratch allocation is not 16-byte aligned");
+  CK(launch_pack_charges(prec, N, n_pad, dx, dq, packed, s), "pack charges");
+  TopoParams p;
+  p.n_lines = L;
+  p.n_charges = N;
+  p.step = step;
+  for (int k = 0; k < 3; ++k) p.half[k] = half[k];
+  p.starts = ds;
+  p.n_iter = dn;
+  p.packed = packed;
+  p.result = dres;
+  p.ends = dends;
+  p.steps = dsteps;
+  p.queue = queue;
+  p.status = c->status;
+  CK(launch_topo(prec, p, c->sms, s), "topo kernel launch");
+  if (mem == CPETGB_HOST) {
+    CK(cudaMemcpyAsync(result, dres, size_t(L) * 2 * sizeof(double), cudaMemcpyDeviceToHost, s),
+       "copy result");
+    if (ends)
+      CK(cudaMemcpyAsync(ends, dends, size_t(L) * 3 * sizeof(double), cudaMemcpyDeviceToHost, s),
+         "copy ends");
+    if (steps)
+      CK(cudaMemcpyAsync(steps, dsteps, size_t(L) * sizeof(int32_t), cudaMemcpyDeviceToHost, s),
+         "copy steps");
+    return finish(c, s);
+  }
+  return CPETGB_OK;
+}
+
+int hist_impl(int mem, int L, const double* result, int nb0, int nb1, const double* range,
+              uint64_t* counts, double* edges, void* stream) {
+  if (!valid_mem(mem)) return fail(CPETGB_EINVAL, "bad memory kind %d", mem);
+  if (L < 0 || nb0 < 1 || nb1 < 1 || nb0 + nb1 > 4096)
+    return fail(CPETGB_EINVAL, "bad histogram shape (%d lines, %d x %d bins)", L, nb0, nb1);
+  if (!range || !counts || (L > 0 && !result)) return fail(CPETGB_EINVAL, "NULL pointer");
+  int rc;
+  Ctx* c = context(&rc);
+  if (!c) return rc;
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  if (mem == CPETGB_HOST && !s) s = c->stream;
+  Scratch S(s);
+  const double* dv = result;
+  unsigned long long* dc = reinterpret_cast<unsigned long long*>(counts);
+  double* de = edges;
+  const size_t nbins = size_t(nb0) * nb1;
+  if (mem == CPETGB_HOST) {
+    if (L) CK(h2d(const_cast<double**>(&dv), S, result, size_t(L) * 2), "copy values");
+    CK(S.get(&dc, nbins), "alloc counts");
+  }
+  if (mem == CPETGB_HOST || !edges) CK(S.get(&de, size_t(nb0 + nb1 + 2)), "alloc edges");
+  CK(cudaMemsetAsync(dc, 0, nbins * sizeof(unsigned long long), s), "zero counts");
+  CK(launch_hist2d(L, dv, nb0, nb1, range, de, dc, c->status, s), "histogram launch");
+  if (mem == CPETGB_HOST) {
+    CK(cudaMemcpyAsync(counts, dc, nbins * sizeof(uint64_t), cudaMemcpyDeviceToHost, s),
+       "copy counts");
+    if (edges)
+      CK(cudaMemcpyAsync(edges, de, size_t(nb0 + nb1 + 2) * sizeof(double),
+                         cudaMemcpyDeviceToHost, s),
+         "copy edges");
+    return finish(c, s);
+  }
+  return CPETGB_OK;
+}
+
+std::vector<double> widen(const float* p, size_t n) {
+  std::vector<double> v(n);
+  for (size_t i = 0; i < n; ++i) v[i] = p[i];
+  return v;
+}
+
+}  // namespace
+
+extern "C" {
+
+int cpetgb_version(void) { return kVersion; }
+
+int cpetgb_last_error(char* buf, size_t len) {
+  if (!buf || len == 0) return CPETGB_EINVAL;
+  std::snprintf(buf, len, "%s", g_err.c_str());
+  return CPETGB_OK;
+}
+
+int cpetgb_device_sms(void) {
+  int rc;
+  Ctx* c = context(&rc);
+  return c ? c->sms : rc;
+}
+
+int cpetgb_synchronize(void* stream) {
+  int rc;
+  Ctx* c = context(&rc);
+  if (!c) return rc;
+  return finish(c, static_cast<cudaStream_t>(stream));
+}
+
+int cpetgb_set_default_precision(int precision) {
+  if (!valid_prec(precision)) return fail(CPETGB_EINVAL, "bad precision %d", precision);
+  g_default_prec.store(precision);
+  return CPETGB_OK;
+}
+
+int cpetgb_get_default_precision(void) { return g_default_prec.load(); }
+
+int cpetgb_field_grid(int precision, int mem, int n_points, int n_charges, const double* points,
+                      const double* x, const double* q, int clamp, double* field, void* stream) {
+  if (n_points < 0 || n_charges < 0) return fail(CPETGB_EINVAL, "negative size");
+  const int64_t desc[4] = {0, n_charges, 0, n_points};
+  return grid_batch_impl(CPETGB_FIELD, precision, mem, clamp, 1, desc, points, x, q, field, stream);
+}
+
+int cpetgb_esp_grid(int precision, int mem, int n_points, int n_charges, const double* points,
+                    const double* x, const double* q, double* esp, void* stream) {
+  if (n_points < 0 || n_charges < 0) return fail(CPETGB_EINVAL, "negative size");
+  const int64_t desc[4] = {0, n_charges, 0, n_points};
+  return grid_batch_impl(CPETGB_ESP, precision, mem, 0, 1, desc, points, x, q, esp, stream);
+}
+
+int cpetgb_grid_batch(int kind, int precision, int mem, int clamp, int n_frames,
+                      const int64_t* desc, const double* points, const double* x,
+                      const double* q, double* out, void* stream) {
+  return grid_batch_impl(kind, precision, mem, clamp, n_frames, desc, points, x, q, out, stream);
+}
+
+int cpetgb_topo_lines(int precision, int mem, int n_lines, int n_charges, const double* starts,
+                      const int32_t* n_iter, double step, const double* half_dims,
+                      const double* x, const double* q, double* result, double* ends,
+                      int32_t* steps, void* stream) {
+  return topo_impl(precision, mem, n_lines, n_charges, starts, n_iter, step, half_dims, x, q,
+                   result, ends, steps, stream);
+}
+
+int cpetgb_topo_hist2d(int mem, int n_lines, const double* result, int nb_dist, int nb_curv,
+                       const double* range, uint64_t* counts, double* edges, void* stream) {
+  return hist_impl(mem, n_lines, result, nb_dist, nb_curv, range, counts, edges, stream);
+}
+
+// ---- float32 drop-ins ----------------------------------------------------
+
+int cpetgb_compute_looped_field(int total_points, int n_charges, const float* x_0,
+                                const float* x, const float* Q, float* E) {
+  if (total_points < 0 || n_charges < 0) return fail(CPETGB_EINVAL, "negative size");
+  if (total_points == 0) return CPETGB_OK;
+  if (!x_0 || !E || (n_charges && (!x || !Q))) return fail(CPETGB_EINVAL, "NULL pointer");
+  auto p = widen(x_0, size_t(total_points) * 3);
+  auto xx = widen(x, size_t(n_charges) * 3);
+  auto qq = widen(Q, size_t(n_charges));
+  std::vector<double> out(size_t(total_points) * 3);
+  const int rc = cpetgb_field_grid(g_default_prec.load(), CPETGB_HOST, total_points, n_charges,
+                                   p.data(), xx.data(), qq.data(), 1, out.data(), nullptr);
+  if (rc != CPETGB_OK) return rc;
+  for (size_t i = 0; i < out.size(); ++i) E[i] = static_cast<float>(out[i]);
+  return CPETGB_OK;
+}
+
+int cpetgb_compute_esp_grid(int total_points, int n_charges, const float* x_0, const float* x,
+                            const float* Q, float* ESP) {
+  if (total_points < 0 || n_charges < 0) return fail(CPETGB_EINVAL, "negative size");
+  if (total_points == 0) return CPETGB_OK;
+  if (!x_0 || !ESP || (n_charges && (!x || !Q))) return fail(CPETGB_EINVAL, "NULL pointer");
+  auto p = widen(x_0, size_t(total_points) * 3);
+  auto xx = widen(x, size_t(n_charges) * 3);
+  auto qq = widen(Q, size_t(n_charges));
+  std::vector<double> out(static_cast<size_t>(total_points));
+  const int rc = cpetgb_esp_grid(g_default_prec.load(), CPETGB_HOST, total_points, n_charges,
+                                 p.data(), xx.data(), qq.data(), out.data(), nullptr);
+  if (rc != CPETGB_OK) return rc;
+  for (size_t i = 0; i < out.size(); ++i) ESP[i] = static_cast<float>(out[i]);
+  return CPETGB_OK;
+}
+
+int cpetgb_calc_esp_base(float* ESP, const float* x_init, int n_charges, const float* x,
+                         const float* Q) {
+  if (!ESP || !x_init) return fail(CPETGB_EINVAL, "NULL pointer");
+  float v = 0.f;
+  const int rc = cpetgb_compute_esp_grid(1, n_charges, x_init, x, Q, &v);
+  if (rc != CPETGB_OK) return rc;
+  ESP[0] += v;
+  return CPETGB_OK;
+}
+
+int cpetgb_calc_field(float* E, const float* x_init, int n_charges, const float* x,
+                      const float* Q) {
+  if (!E || !x_init) return fail(CPETGB_EINVAL, "NULL pointer");
+  if (n_charges < 0) return fail(CPETGB_EINVAL, "negative size");
+  double p[3] = {x_init[0], x_init[1], x_init[2]}, out[3];
+  auto xx = widen(x, size_t(n_charges) * 3);
+  auto qq = widen(Q, size_t(n_charges));
+  const int rc = cpetgb_field_grid(g_default_prec.load(), CPETGB_HOST, 1, n_charges, p, xx.data(),
+                                   qq.data(), 0, out, nullptr);
+  if (rc != CPETGB_OK) return rc;
+  for (int k = 0; k < 3; ++k) E[k] = static_cast<float>(out[k]);
+  return CPETGB_OK;
+}
+
+int cpetgb_thread_operation_batch(int n_lines, int n_charges, const int32_t* n_iter,
+                                  float step_size, const float* x_0, const float* dimensions,
+                                  const float* x, const float* Q, float* ret) {
+  if (n_lines < 0 || n_charges < 0) return fail(CPETGB_EINVAL, "negative size");
+  if (n_lines == 0) return CPETGB_OK;
+  if (!n_iter || !x_0 || !dimensions || !ret || (n_charges && (!x || !Q)))
+    return fail(CPETGB_EINVAL, "NULL pointer");
+  auto s = widen(x_0, size_t(n_lines) * 3);
+  auto xx = widen(x, size_t(n_charges) * 3);
+  auto qq = widen(Q, size_t(n_charges));
+  const double half[3] = {dimensions[0], dimensions[1], dimensions[2]};
+  std::vector<double> res(size_t(n_lines) * 2);
+  const int rc = cpetgb_topo_lines(g_default_prec.load(), CPETGB_HOST, n_lines, n_charges,
+                                   s.data(), n_iter, double(step_size), half, xx.data(),
+                                   qq.data(), res.data(), nullptr, nullptr, nullptr);
+  if (rc != CPETGB_OK) return rc;
+  for (size_t i = 0; i < res.size(); ++i) ret[i] = static_cast<float>(res[i]);
+  return CPETGB_OK;
+}
+
+int cpetgb_thread_operation(int n_charges, int n_iter, float step_size, const float* x_0,
+                            const float* dimensions, const float* x, const float* Q,
+                            float* ret) {
+  const int32_t it = n_iter;
+  return cpetgb_thread_operation_batch(1, n_charges, &it, step_size, x_0, dimensions, x, Q, ret);
+}
+
+}  // extern "C"

@@ -1,0 +1,275 @@
+// grid.cu -- all-pairs Coulomb sums on point sets (K1 field, K2 potential).
+//
+// Replaces compute_looped_field (CPET/utils/math_module.c:405-451, field with
+// r^2 clamped at 1e-6), calc_field (math_module.c:255-293, unclamped field at
+// a point) and calc_esp_base (math_module.c:453-486, potential), which the
+// reference evaluates one point at a time on one CPU core.
+//
+// Work decomposition: a CTA owns one GridItem = a tile of kGridTilePts points
+// of one frame (kGridPPT points per thread, kept in registers) and a contiguous
+// range of that frame's charges.  The charges stream through a ring of shared
+// memory stages filled by 1-D bulk async copies (cp.async.bulk) that complete
+// on mbarriers; every thread reads each staged charge as a broadcast and
+// applies it to its kGridPPT points.
+//
+// Precision forms:
+//   FP32C  pair terms in FP32 with the MUFU rsqrt; each stage's contribution is
+//          summed plainly in FP32 and then Kahan-added (compensated) into a
+//          running (sum, compensation) pair per component; the result leaves
+//          the CTA as a double.
+//   FP64   every operation in IEEE double (plain sums), the drop-in form.
+// A frame whose charges are split over several items writes per-split partial
+// sums (doubles) that grid_final_kernel adds in split order: deterministic.
+#include <algorithm>
+#include <type_traits>
+
+#include "common.cuh"
+#include "kernels.cuh"
+
+namespace cpetgb {
+namespace {
+
+constexpr int kStages = 4;
+
+template <int PREC>
+struct GridCfg;
+template <>
+struct GridCfg<kFP32C> {
+  using ChargeT = float4;
+  using Real = float;
+  static constexpr int kTile = 512;  // charges per stage (8 KiB)
+};
+template <>
+struct GridCfg<kFP64> {
+  using ChargeT = Charge64;
+  using Real = double;
+  static constexpr int kTile = 256;  // charges per stage (8 KiB)
+};
+
+__device__ __forceinline__ double rsqrt_f64(double x) { return rsqrt(x); }
+__device__ __forceinline__ float charge_q(const float4& c) { return c.w; }
+__device__ __forceinline__ double charge_q(const Charge64& c) { return c.q; }
+
+template <int PREC, int KIND, bool CLAMP>
+__global__ void __launch_bounds__(kGridThreads)
+    grid_kernel(const GridItem* __restrict__ items, const void* __restrict__ packed,
+                const double* __restrict__ points, double* __restrict__ out,
+                double* __restrict__ partial, int* __restrict__ status) {
+  using Cfg = GridCfg<PREC>;
+  using ChargeT = typename Cfg::ChargeT;
+  using Real = typename Cfg::Real;
+  constexpr int TC = Cfg::kTile;
+  constexpr int NC = (KIND == kField) ? 3 : 1;
+
+  __shared__ alignas(128) ChargeT tile[kStages][TC];
+  __shared__ alignas(8) uint64_t full[kStages];
+
+  const GridItem it = items[blockIdx.x];
+  const ChargeT* src = reinterpret_cast<const ChargeT*>(packed) + it.charge_off + it.n_begin;
+  const int n = it.n_count;
+  const int n_tiles = (n + TC - 1) / TC;
+  const int tid = threadIdx.x;
+
+  if (tid == 0) {
+    for (int s = 0; s < kStages; ++s) mbar_init(&full[s], 1);
+    fence_mbar_init();
+  }
+  __syncthreads();
+
+  auto issue = [&](int t) {
+    const int s = t % kStages;
+    const int cnt = min(TC, n - t * TC);
+    const uint32_t bytes = static_cast<uint32_t>(cnt * sizeof(ChargeT));
+    mbar_arrive_expect_tx(&full[s], bytes);
+    bulk_g2s(&tile[s][0], src + static_cast<int64_t>(t) * TC, bytes, &full[s]);
+  };
+  if (tid == 0) {
+    for (int t = 0; t < min(kStages, n_tiles); ++t) issue(t);
+  }
+
+  // This thread's points, in registers.
+  Real px[kGridPPT], py[kGridPPT], pz[kGridPPT];
+#pragma unroll
+  for (int k = 0; k < kGridPPT; ++k) {
+    const int pl = tid + k * kGridThreads;
+    if (pl < it.p_count) {
+      const double* pp = points + 3 * (it.point_off + it.p_begin + pl);
+      px[k] = static_cast<Real>(pp[0]);
+      py[k] = static_cast<Real>(pp[1]);
+      pz[k] = static_cast<Real>(pp[2]);
+    } else {
+      px[k] = py[k] = pz[k] = static_cast<Real>(1.0e4);  // far away, never written
+    }
+  }
+
+  // Running sums: acc = sum, cmp = Kahan compensation (FP32C only).
+  Real acc[NC][kGridPPT], cmp[NC][kGridPPT];
+#pragma unroll
+  for (int c = 0; c < NC; ++c)
+#pragma unroll
+    for (int k = 0; k < kGridPPT; ++k) acc[c][k] = cmp[c][k] = Real(0);
+
+  bool ok = true;
+  for (int t = 0; t < n_tiles; ++t) {
+    const int s = t % kStages;
+    const bool mine = mbar_wait(&full[s], static_cast<uint32_t>((t / kStages) & 1), status);
+    ok = __syncthreads_and(mine) != 0;  // also: every thread is done with tile t-1
+    if (!ok) break;
+    if (tid == 0 && t >= 1 && (t - 1) + kStages < n_tiles) issue((t - 1) + kStages);
+
+    const int cnt = min(TC, n - t * TC);
+    const ChargeT* tl = &tile[s][0];
+    Real part[NC][kGridPPT];
+#pragma unroll
+    for (int c = 0; c < NC; ++c)
+#pragma unroll
+      for (int k = 0; k < kGridPPT; ++k) part[c][k] = Real(0);
+
+#pragma unroll 4
+    for (int j = 0; j < cnt; ++j) {
+      const ChargeT ch = tl[j];
+#pragma unroll
+      for (int k = 0; k < kGridPPT; ++k) {
+        const Real dx = px[k] - ch.x;
+        const Real dy = py[k] - ch.y;
+        const Real dz = pz[k] - ch.z;
+        Real r2 = dx * dx + dy * dy + dz * dz;
+        if constexpr (CLAMP) r2 = fmax(r2, Real(1e-6));  // compute_looped_field's fmaxf
+        Real ri;
+        if constexpr (PREC == kFP32C)
+          ri = rsqrt_mufu(r2);
+        else
+          ri = rsqrt_f64(r2);
+        if constexpr (KIND == kField) {
+          const Real w = (charge_q(ch) * ri) * (ri * ri);
+          part[0][k] += w * dx;
+          part[1][k] += w * dy;
+          part[2][k] += w * dz;
+        } else {
+          part[0][k] += charge_q(ch) * ri;
+        }
+      }
+    }
+#pragma unroll
+    for (int c = 0; c < NC; ++c)
+#pragma unroll
+      for (int k = 0; k < kGridPPT; ++k) {
+        if constexpr (PREC == kFP32C)
+          kahan_add(acc[c][k], cmp[c][k], part[c][k]);
+        else
+          acc[c][k] += part[c][k];
+      }
+  }
+  if (!ok) return;
+
+#pragma unroll
+  for (int k = 0; k < kGridPPT; ++k) {
+    const int pl = tid + k * kGridThreads;
+    if (pl >= it.p_count) continue;
+#pragma unroll
+    for (int c = 0; c < NC; ++c) {
+      const double v =
+          (static_cast<double>(acc[c][k]) - static_cast<double>(cmp[c][k])) * kCoulomb;
+      if (it.slot < 0) {
+        out[NC * (it.point_off + it.p_begin + pl) + c] = v;
+      } else {
+        partial[(static_cast<int64_t>(it.slot) * kGridTilePts + pl) * 3 + c] = v;
+      }
+    }
+  }
+}
+
+template <int KIND>
+__global__ void grid_final_kernel(const GridFinal* __restrict__ fin,
+                                  const double* __restrict__ partial, double* __restrict__ out) {
+  constexpr int NC = (KIND == kField) ? 3 : 1;
+  const GridFinal f = fin[blockIdx.x];
+  for (int i = threadIdx.x; i < f.p_count * NC; i += blockDim.x) {
+    const int pl = i / NC, c = i % NC;
+    double v = 0.0;
+    for (int s = 0; s < f.n_split; ++s)
+      v += partial[(static_cast<int64_t>(f.slot_base + s) * kGridTilePts + pl) * 3 + c];
+    out[NC * (f.out_row + pl) + c] = v;
+  }
+}
+
+__global__ void pack_f32_kernel(int64_t n, int64_t n_pad, const double* __restrict__ x,
+                                const double* __restrict__ q, float4* __restrict__ out) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n_pad;
+       i += (int64_t)gridDim.x * blockDim.x)
+    out[i] = i < n ? make_float4(static_cast<float>(x[3 * i]), static_cast<float>(x[3 * i + 1]),
+                                 static_cast<float>(x[3 * i + 2]), static_cast<float>(q[i]))
+                   : make_float4(1.0e4f, 1.0e4f, 1.0e4f, 0.f);
+}
+
+__global__ void pack_f64_kernel(int64_t n, int64_t n_pad, const double* __restrict__ x,
+                                const double* __restrict__ q, Charge64* __restrict__ out) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n_pad;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    Charge64 c;
+    if (i < n) {
+      c.x = x[3 * i];
+      c.y = x[3 * i + 1];
+      c.z = x[3 * i + 2];
+      c.q = q[i];
+    } else {
+      c.x = c.y = c.z = 1.0e4;
+      c.q = 0.0;
+    }
+    out[i] = c;
+  }
+}
+
+template <int PREC, int KIND>
+cudaError_t launch_grid_t(int clamp, int n_items, const GridItem* items, const void* packed,
+                          const double* points, double* out, double* partial, int* status,
+                          cudaStream_t s) {
+  if (clamp)
+    grid_kernel<PREC, KIND, true>
+        <<<n_items, kGridThreads, 0, s>>>(items, packed, points, out, partial, status);
+  else
+    grid_kernel<PREC, KIND, false>
+        <<<n_items, kGridThreads, 0, s>>>(items, packed, points, out, partial, status);
+  return cudaGetLastError();
+}
+
+}  // namespace
+
+cudaError_t launch_pack_charges(int prec, int64_t n, int64_t n_pad, const double* x,
+                                const double* q, void* packed, cudaStream_t s) {
+  if (n_pad <= 0) return cudaSuccess;
+  const int blocks = static_cast<int>(std::min<int64_t>((n_pad + 255) / 256, 4096));
+  if (prec == kFP32C)
+    pack_f32_kernel<<<blocks, 256, 0, s>>>(n, n_pad, x, q, static_cast<float4*>(packed));
+  else
+    pack_f64_kernel<<<blocks, 256, 0, s>>>(n, n_pad, x, q, static_cast<Charge64*>(packed));
+  return cudaGetLastError();
+}
+
+cudaError_t launch_grid(int prec, int kind, int clamp, int n_items, const GridItem* items,
+                        const void* packed, const double* points, double* out, double* partial,
+                        int* status, cudaStream_t s) {
+  if (n_items <= 0) return cudaSuccess;
+  if (prec == kFP32C) {
+    return kind == kField ? launch_grid_t<kFP32C, kField>(clamp, n_items, items, packed, points,
+                                                         out, partial, status, s)
+                          : launch_grid_t<kFP32C, kEsp>(0, n_items, items, packed, points, out,
+                                                       partial, status, s);
+  }
+  return kind == kField ? launch_grid_t<kFP64, kField>(clamp, n_items, items, packed, points, out,
+                                                      partial, status, s)
+                        : launch_grid_t<kFP64, kEsp>(0, n_items, items, packed, points, out,
+                                                    partial, status, s);
+}
+
+cudaError_t launch_grid_final(int kind, int n_final, const GridFinal* fin, const double* partial,
+                              double* out, cudaStream_t s) {
+  if (n_final <= 0) return cudaSuccess;
+  if (kind == kField)
+    grid_final_kernel<kField><<<n_final, 256, 0, s>>>(fin, partial, out);
+  else
+    grid_final_kernel<kEsp><<<n_final, 256, 0, s>>>(fin, partial, out);
+  return cudaGetLastError();
+}
+
+}  // namespace cpetgb

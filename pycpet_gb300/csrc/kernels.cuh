@@ -1,0 +1,92 @@
+// kernels.cuh -- launch interface between the C-ABI layer (api.cu) and the
+// kernels (grid.cu, topo.cu, hist.cu).  Host-side declarations only.
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace cpetgb {
+
+enum Precision : int { kFP64 = 0, kFP32C = 1 };
+
+// Status word written by kernels (device memory); 0 = fine, first error wins.
+enum DevStatus : int {
+  kDevOk = 0,
+  kDevWaitTimeout = 1,   // an mbarrier wait exceeded its limit
+  kDevBadArgument = 2,   // histogram range not finite or inverted
+  kDevBadCap = 3,        // a streamline step cap above kMaxLineCap
+};
+
+// Largest accepted per-line step cap: keeps every streamline kernel bounded.
+constexpr int kMaxLineCap = 1 << 24;
+enum GridKind : int { kField = 0, kEsp = 1 };
+
+// Packed charge layouts in HBM (positions relative to the box centre).
+struct alignas(32) Charge64 {
+  double x, y, z, q;
+};
+// FP32C uses float4 {x, y, z, q}.
+
+// One CTA of the grid kernel: a tile of up to kGridTilePts points of one frame
+// against a contiguous range of that frame's charges.
+struct GridItem {
+  int64_t charge_off;  // first packed charge of the frame
+  int64_t point_off;   // first point of the frame (points / output rows)
+  int32_t p_begin;     // first point of this tile inside the frame
+  int32_t p_count;     // points in this tile (<= kGridTilePts)
+  int32_t n_begin;     // first charge of this item inside the frame
+  int32_t n_count;     // charges of this item
+  int32_t slot;        // partial-sum slot (>= 0), or -1 to write the final value
+  int32_t pad;
+};
+static_assert(sizeof(GridItem) == 40, "GridItem layout");
+
+// Reduction of the partial sums of one point tile over its charge splits.
+struct GridFinal {
+  int64_t out_row;     // first output row (frame point_off + p_begin)
+  int32_t p_count;
+  int32_t slot_base;   // partial slots slot_base .. slot_base + n_split - 1
+  int32_t n_split;
+  int32_t pad;
+};
+static_assert(sizeof(GridFinal) == 24, "GridFinal layout");
+
+constexpr int kGridThreads = 128;
+constexpr int kGridPPT = 4;  // points per thread
+constexpr int kGridTilePts = kGridThreads * kGridPPT;
+
+// grid.cu
+// Packs x[n][3], q[n] into float4 / Charge64 and fills [n, n_pad) with zero
+// charges placed far outside any box (they contribute exactly zero).
+cudaError_t launch_pack_charges(int prec, int64_t n, int64_t n_pad, const double* x,
+                                const double* q, void* packed, cudaStream_t s);
+cudaError_t launch_grid(int prec, int kind, int clamp, int n_items, const GridItem* items,
+                        const void* packed, const double* points, double* out,
+                        double* partial, int* status, cudaStream_t s);
+cudaError_t launch_grid_final(int kind, int n_final, const GridFinal* fin,
+                              const double* partial, double* out, cudaStream_t s);
+
+// topo.cu
+struct TopoParams {
+  int n_lines;
+  int n_charges;
+  double step;
+  double half[3];
+  const double* starts;      // [L][3]
+  const int32_t* n_iter;     // [L]
+  const void* packed;        // packed charges
+  double* result;            // [L][2]  {distance, mean curvature}
+  double* ends;              // [L][3] or null
+  int32_t* steps;            // [L] or null (Euler steps of the main loop)
+  int* queue;                // work-queue counter (zeroed by the launcher)
+  int* status;
+};
+cudaError_t launch_topo(int prec, const TopoParams& p, int num_sms, cudaStream_t s);
+size_t topo_resident_limit(int prec);  // max charges held resident in shared memory
+int topo_charge_pad();                 // packed charge arrays are padded to this multiple
+
+// hist.cu
+cudaError_t launch_hist2d(int n, const double* vals, int nb0, int nb1, const double* range,
+                          double* edges, unsigned long long* counts, int* status,
+                          cudaStream_t s);
+
+}  // namespace cpetgb

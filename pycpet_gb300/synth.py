@@ -1,0 +1,84 @@
+"""Seeded synthetic frames with the shapes and value distributions of the
+benchmark workloads (no protein files ship with the benchmarks).
+
+A frame is a set of point charges already expressed in the box frame (centre at
+the origin, axes from three seeded atoms), exactly what PyCPET's ``calculator``
+holds in ``self.x`` / ``self.Q`` after its rotation step
+(CPET/source/calculator.py:341-346):
+
+* positions uniform in a cube of edge 50 A (5,000 charges) scaled as
+  50 * (N/5000)^(1/3) A for other N, i.e. a density of 0.04 charges / A^3;
+* a minimum pair separation of 1.0 A (rejection sampling with a k-d tree);
+* no charge within 2.0 A of the box centre;
+* partial charges ~ N(0, 0.4) clipped to +-1, then shifted by one constant so
+  the net charge is the nearest integer.
+
+All randomness comes from ``numpy.random.default_rng(seed)`` so the same frame
+is produced on every machine.
+"""
+from __future__ import annotations
+
+import numpy as np
+
+from .calculator import box_transformation
+
+
+def cube_edge(n_charges: int) -> float:
+    return 50.0 * (n_charges / 5000.0) ** (1.0 / 3.0)
+
+
+def _sample_positions(rng, n, edge, min_sep, exclude_r):
+    from scipy.spatial import cKDTree
+
+    accepted = np.empty((0, 3))
+    half = edge / 2.0
+    while len(accepted) < n:
+        need = n - len(accepted)
+        cand = rng.uniform(-half, half, size=(int(need * 1.3) + 16, 3))
+        cand = cand[np.linalg.norm(cand, axis=1) >= exclude_r]
+        if len(accepted):
+            d, _ = cKDTree(accepted).query(cand, k=1)
+            cand = cand[d >= min_sep]
+        # resolve conflicts inside the batch: keep the earlier candidate of each pair
+        if len(cand) > 1:
+            pairs = cKDTree(cand).query_pairs(min_sep, output_type="ndarray")
+            if len(pairs):
+                drop = np.zeros(len(cand), bool)
+                for a, b in pairs[np.argsort(pairs[:, 1], kind="stable")]:
+                    if not drop[a]:
+                        drop[b] = True
+                cand = cand[~drop]
+        accepted = np.concatenate([accepted, cand[:need]])
+    return accepted
+
+
+def make_charges(n_charges: int, seed: int, edge: float | None = None, min_sep: float = 1.0,
+                 exclude_r: float = 2.0, sigma: float = 0.4):
+    """Returns (x (N,3) float64, q (N,) float64) in the lab frame, centre at origin."""
+    rng = np.random.default_rng(seed)
+    edge = cube_edge(n_charges) if edge is None else edge
+    x = _sample_positions(rng, n_charges, edge, min_sep, exclude_r)
+    q = np.clip(rng.normal(0.0, sigma, n_charges), -1.0, 1.0)
+    q = q + (np.round(q.sum()) - q.sum()) / n_charges
+    return x, q
+
+
+def make_frame(n_charges: int, seed: int, edge: float | None = None):
+    """Charges rotated into the box frame built from three seeded atoms.
+
+    Returns dict(x=(N,3) f64, q=(N,) f64, T=(3,3) box basis, seed=seed).
+    """
+    x, q = make_charges(n_charges, seed, edge)
+    rng = np.random.default_rng(seed + 7919)
+    a, b = rng.choice(n_charges, size=2, replace=False)
+    T = box_transformation(np.zeros(3), x[a], x[b])
+    x_local = x @ np.linalg.inv(T)
+    return {"x": np.ascontiguousarray(x_local), "q": q, "T": T, "seed": seed}
+
+
+def random_start_points(n_lines: int, half_widths, seed: int):
+    """Seeded uniform start points inside the box (the 'random' initializer,
+    CPET/utils/calculator.py:155-159, with a seeded generator)."""
+    rng = np.random.default_rng(seed)
+    hw = np.asarray(half_widths, dtype=np.float64)
+    return np.column_stack([rng.uniform(-hw[k], hw[k], n_lines) for k in range(3)])

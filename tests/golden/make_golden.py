@@ -1,0 +1,176 @@
+"""Generates the golden fixtures of tests/golden from the reference itself.
+
+Needs a checkout of pujanajmera/pycpet (``--ref``, default /root/reference) and
+its C library compiled from source by ``make -C oracle`` (into
+oracle/_ref/math_module.so; the prebuilt binaries shipped in the checkout are
+never loaded).  Third-party modules the reference imports but this path does
+not use (numba, matplotlib, kneed, tensorly, pandas, seaborn) are stubbed.
+
+    make -C oracle && python tests/golden/make_golden.py
+
+Fixtures written (all small, compressed .npz):
+  examples_point_field.npz  examples 1A/1B: the charges of each frame after
+                            the reference's parse/filter/rotate pipeline, the
+                            reference's point field recomputed here and the
+                            values in the shipped outputs point_field.dat
+  ref_grid.npz              a 2,000-charge synthetic frame on an 11^3 grid:
+                            compute_field_on_grid, calc_esp_base per point,
+                            compute_ESP_on_grid (float16) and calc_field
+  ref_topo.npz              192 streamlines of a 1,500-charge synthetic frame
+                            through the reference's compute_topo_complete_c_shared
+  examples_topology.npz     the (distance, curvature) rows of example 3A's
+                            shipped .top files and the reference's
+                            make_histograms of them
+"""
+from __future__ import annotations
+
+import argparse
+import glob
+import importlib.util
+import json
+import os
+import sys
+import types
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+REPO = os.path.dirname(os.path.dirname(HERE))
+REF_SO = os.path.join(REPO, "oracle", "_ref", "math_module.so")
+
+
+def _stub_modules():
+    def mod(name, **attrs):
+        m = types.ModuleType(name)
+        m.__dict__.update(attrs)
+        sys.modules[name] = m
+        return m
+
+    def njit(*a, **k):
+        if a and callable(a[0]) and not k:
+            return a[0]
+        return lambda f: f
+
+    mod("numba", njit=njit, jit=njit, prange=range)
+    mpl = mod("matplotlib")
+    mpl.pyplot = mod("matplotlib.pyplot")
+    mod("mpl_toolkits")
+    mod("mpl_toolkits.mplot3d", Axes3D=object)
+    mod("kneed", KneeLocator=object)
+    tl = mod("tensorly")
+    tl.decomposition = mod("tensorly.decomposition", parafac=None)
+    mod("pandas")
+    mod("seaborn")
+
+
+def import_reference(ref_root):
+    if not os.path.exists(REF_SO):
+        raise SystemExit(f"{REF_SO} missing: run `make -C oracle` first")
+    _stub_modules()
+    orig = importlib.util.find_spec
+
+    def find_spec(name, *a, **k):  # point the reference at the library built from source
+        if name == "CPET.utils.math_module":
+            return types.SimpleNamespace(origin=REF_SO)
+        return orig(name, *a, **k)
+
+    importlib.util.find_spec = find_spec
+    sys.path.insert(0, ref_root)
+    import CPET.utils.calculator as ucalc
+    import CPET.source.calculator as scalc
+
+    return ucalc, scalc
+
+
+def examples_point_field(ref_root, scalc, out):
+    rec = {}
+    for ex in ("1A_point-field", "1B_point-field-oriented"):
+        with open(os.path.join(ref_root, "examples", ex, "options", "options.json")) as fh:
+            opts = json.load(fh)
+        shipped = {}
+        with open(os.path.join(ref_root, "examples", ex, "outdir", "point_field.dat")) as fh:
+            for line in fh:
+                name, vec = line.strip().split(":", 1)
+                shipped[name] = np.array(vec.strip("[] \n").split(), dtype=np.float64)
+        for pdb in sorted(glob.glob(os.path.join(ref_root, "examples", "1A_point-field", "pdb", "*.pdb"))):
+            name = os.path.basename(pdb).split(".")[0]
+            calc = scalc.calculator(dict(opts), path_to_pdb=pdb)
+            E = calc.compute_point_field()
+            key = f"{ex[:2]}_{name}"
+            rec[f"{key}_x"] = np.asarray(calc.x, np.float32)
+            rec[f"{key}_Q"] = np.asarray(calc.Q, np.float32).reshape(-1)
+            rec[f"{key}_E_ref"] = np.asarray(E, np.float32)
+            rec[f"{key}_E_shipped"] = shipped[name]
+    np.savez_compressed(out, **rec)
+    return rec
+
+
+def ref_grid(ucalc, out):
+    sys.path.insert(0, REPO)
+    from pycpet_gb300.synth import make_frame
+
+    fr = make_frame(2000, seed=11)
+    x = fr["x"].astype(np.float32)
+    Q = fr["q"].astype(np.float32).reshape(-1, 1)
+    mesh, _ = ucalc.initialize_box_points_uniform(center=np.zeros(3), x=np.array([1.0, 0, 0]),
+                                                  y=np.array([0, 1.0, 0]), N_cr=[10, 10, 10],
+                                                  dimensions=[1.0, 1.0, 1.0], dtype="float32", inclusive=True)
+    field = ucalc.compute_field_on_grid(mesh, x, Q)
+    pts = mesh.reshape(-1, 3)
+    esp = np.array([ucalc.calculate_esp_c_shared_full(p, x, Q)[0] for p in pts], dtype=np.float32)
+    esp_half = ucalc.compute_ESP_on_grid(mesh, x, Q)
+    pf = ucalc.calculate_electric_field_c_shared_full_alt(np.array([0.0, 0.0, 0.0]), x, Q)
+    np.savez_compressed(out, x=x, Q=Q.reshape(-1), mesh=mesh, field=field, esp=esp, esp_half=esp_half,
+                        point_field=np.asarray(pf, np.float32))
+
+
+def ref_topo(scalc, out):
+    from pycpet_gb300.synth import make_frame, random_start_points
+
+    fr = make_frame(1500, seed=12)
+    dims = np.array([1.5, 1.5, 1.5], dtype=np.float32)
+    step = 0.01
+    starts = random_start_points(192, dims, seed=13).astype(np.float32)
+    max_steps = round(2 * np.linalg.norm(dims) / step)
+    caps = np.random.default_rng(14).integers(1, max_steps, 192)
+    calc = scalc.calculator.__new__(scalc.calculator)
+    calc.x = fr["x"].astype(np.float32)
+    calc.Q = fr["q"].astype(np.float32).reshape(-1, 1)
+    calc.random_start_points = starts
+    calc.random_max_samples = caps
+    calc.step_size = step
+    calc.dimensions = dims
+    calc.n_samples = len(starts)
+    calc.concur_slip = 4
+    calc.transformation_matrix = np.eye(3)
+    calc.center = np.zeros(3, np.float32)
+    calc.log = scalc.log
+    hist = calc.compute_topo_complete_c_shared()
+    np.savez_compressed(out, x=calc.x, Q=calc.Q.reshape(-1), starts=starts, caps=caps.astype(np.int32),
+                        dims=dims, step=np.float32(step), result=np.asarray(hist, np.float32))
+
+
+def examples_topology(ref_root, ucalc, out):
+    files = sorted(glob.glob(os.path.join(ref_root, "examples", "3A_field-topology", "outdir", "*.top")))
+    rec = {}
+    for i, f in enumerate(files):
+        rec[f"top{i}"] = np.loadtxt(f)
+    rec["hist"] = ucalc.make_histograms(files)
+    np.savez_compressed(out, **rec)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--ref", default="/root/reference")
+    a = ap.parse_args()
+    ucalc, scalc = import_reference(a.ref)
+    examples_point_field(a.ref, scalc, os.path.join(HERE, "examples_point_field.npz"))
+    ref_grid(ucalc, os.path.join(HERE, "ref_grid.npz"))
+    ref_topo(scalc, os.path.join(HERE, "ref_topo.npz"))
+    examples_topology(a.ref, ucalc, os.path.join(HERE, "examples_topology.npz"))
+    for f in sorted(glob.glob(os.path.join(HERE, "*.npz"))):
+        print(f, os.path.getsize(f))
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,64 @@
+"""The C-ABI library builds, loads and exports every symbol include/cpetgb.h
+declares; the Python binding declares every one of them; without a GPU the
+library refuses work instead of falling back to the CPU."""
+import ctypes
+import os
+import re
+
+import pytest
+
+from conftest import ROOT
+
+
+def header_symbols():
+    with open(os.path.join(ROOT, "include", "cpetgb.h")) as fh:
+        text = fh.read()
+    return sorted(set(re.findall(r"^\s*int\s+(cpetgb_\w+)\s*\(", text, flags=re.M)))
+
+
+@pytest.fixture(scope="module")
+def built():
+    from pycpet_gb300 import build
+
+    return build.build_library()
+
+
+def test_library_exports_header_symbols(built):
+    syms = header_symbols()
+    assert len(syms) >= 17
+    L = ctypes.CDLL(built)
+    missing = [s for s in syms if not hasattr(L, s)]
+    assert not missing, missing
+
+
+def test_binding_covers_header(built):
+    from pycpet_gb300 import _lib
+
+    assert set(header_symbols()) == set(_lib.SIGNATURES)
+    L = _lib.lib()
+    assert L.cpetgb_version() >= 10000
+    assert L.cpetgb_get_default_precision() == _lib.FP32C
+    assert L.cpetgb_set_default_precision(7) == _lib.EINVAL
+    assert "precision" in _lib.last_error()
+
+
+def test_no_cpu_fallback(built):
+    import torch
+
+    if torch.cuda.is_available():
+        pytest.skip("a GPU is present")
+    import numpy as np
+    from pycpet_gb300 import CpetgbError, field_grid
+
+    with pytest.raises(CpetgbError) as e:
+        field_grid(np.zeros((4, 3)), np.ones((2, 3)), np.ones(2))
+    assert e.value.code == -5  # CPETGB_ENODEV
+
+
+def test_argument_validation_before_device(built):
+    """Shape errors are reported as EINVAL before any device work."""
+    from pycpet_gb300 import _lib
+
+    L = _lib.lib()
+    assert L.cpetgb_field_grid(3, 0, 1, 1, None, None, None, 1, None, None) == _lib.EINVAL
+    assert L.cpetgb_topo_hist2d(0, 1, None, 0, 20, None, None, None, None) == _lib.EINVAL

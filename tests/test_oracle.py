@@ -1,0 +1,103 @@
+"""Pins the CPU oracle to the reference before it is trusted as a checker.
+
+Golden fixtures (tests/golden, made by make_golden.py from the reference's own
+code and its C library compiled from source):
+  * examples 1A/1B point fields as shipped in the reference's example outputs;
+  * compute_looped_field / calc_esp_base / calc_field on a synthetic grid;
+  * compute_topo_complete_c_shared streamlines on a synthetic frame.
+The FP64 oracle must agree with the FP32 reference to FP32 rounding; the FP32
+restatement must agree with the reference library more tightly still.
+"""
+import os
+
+import numpy as np
+import pytest
+
+
+def _example_keys(d):
+    return sorted({k[: -len("_x")] for k in d.files if k.endswith("_x")})
+
+
+def test_point_field_matches_shipped_examples(golden, oracle):
+    d = golden("examples_point_field.npz")
+    keys = _example_keys(d)
+    assert len(keys) == 4
+    for k in keys:
+        x, Q, shipped = d[k + "_x"], d[k + "_Q"], d[k + "_E_shipped"]
+        E64 = oracle.field_grid_f64(np.zeros((1, 3)), x, Q, clamp=False)[0]
+        # the shipped values are FP32 sums of ~7,900 terms printed to 8 digits
+        np.testing.assert_allclose(E64, shipped, rtol=0, atol=5e-6 * np.abs(shipped).max())
+        E32 = oracle.point_field_f32(np.zeros((1, 3)), x, Q)[0]
+        np.testing.assert_allclose(E32, d[k + "_E_ref"], rtol=0, atol=2e-6 * np.abs(shipped).max())
+
+
+def test_grid_field_and_esp_match_reference(golden, oracle):
+    g = golden("ref_grid.npz")
+    pts = g["mesh"].reshape(-1, 3)
+    E_ref = g["field"][:, 3:]
+    np.testing.assert_array_equal(g["field"][:, :3], pts)
+    E64 = oracle.field_grid_f64(pts, g["x"], g["Q"], clamp=True)
+    scale = np.abs(E_ref).max()
+    assert np.abs(E64 - E_ref).max() <= 1e-5 * scale
+    E32 = oracle.field_grid_f32(pts, g["x"], g["Q"])
+    assert np.abs(E32 - E_ref).max() <= 2e-6 * scale
+    phi64 = oracle.esp_grid_f64(pts, g["x"], g["Q"])
+    assert np.abs(phi64 - g["esp"]).max() <= 1e-5 * np.abs(g["esp"]).max()
+    # compute_ESP_on_grid casts to float16
+    np.testing.assert_array_equal(np.concatenate([pts, g["esp"].reshape(-1, 1)], axis=1).astype(np.half),
+                                  g["esp_half"])
+    pf = oracle.field_grid_f64(np.zeros((1, 3)), g["x"], g["Q"], clamp=False)[0]
+    np.testing.assert_allclose(pf, g["point_field"], rtol=0, atol=1e-5 * np.abs(pf).max())
+
+
+def test_topology_matches_reference(golden, oracle):
+    t = golden("ref_topo.npz")
+    r64, ends, steps = oracle.topo_lines_f64(t["starts"], t["caps"], t["x"], t["Q"], float(t["step"]), t["dims"])
+    R = t["result"]
+    assert np.abs(r64[:, 0] - R[:, 0]).max() < 5e-6          # distance (A)
+    rel = np.abs(r64[:, 1] - R[:, 1]) / np.abs(R[:, 1])
+    # FP32 curvature is a second difference of float positions: noisy
+    assert np.median(rel) < 5e-3 and rel.max() < 5e-2
+    assert steps.min() >= 1 and np.all(steps <= t["caps"])
+    r32, _, _ = oracle.topo_lines_f32(t["starts"], t["caps"], t["x"], t["Q"], float(t["step"]), t["dims"])
+    assert np.abs(r32[:, 0] - R[:, 0]).max() < 5e-6
+
+
+def test_topology_semantics(oracle):
+    """Hand-checkable cases of thread_operation (math_module.c:523-591)."""
+    x = np.array([[0.0, 0.0, 10.0]])
+    q = np.array([1.0])
+    # a single positive charge on +z: field lines point straight down (-z)
+    res, ends, steps = oracle.topo_lines_f64(np.array([[0.0, 0.0, 0.0]]), [1000], x, q, 0.1, [1.0, 1.0, 1.0])
+    assert steps[0] == 11                                     # first point strictly beyond -1.0
+    np.testing.assert_allclose(ends[0], [0, 0, -1.1], atol=1e-12)
+    np.testing.assert_allclose(res[0, 0], 1.1, atol=1e-12)
+    assert abs(res[0, 1]) < 1e-12                             # straight line: zero curvature
+    # cap reached before the box edge
+    res, ends, steps = oracle.topo_lines_f64(np.array([[0.0, 0.0, 0.0]]), [3], x, q, 0.1, [1.0, 1.0, 1.0])
+    assert steps[0] == 3 and abs(res[0, 0] - 0.3) < 1e-12
+    # n_iter = 0: end point = start point
+    res, ends, steps = oracle.topo_lines_f64(np.array([[0.2, 0.0, 0.0]]), [0], x, q, 0.1, [1.0, 1.0, 1.0])
+    assert steps[0] == 0 and res[0, 0] == 0.0
+
+
+def test_reference_library_cross_check(oracle):
+    """Live comparison with the reference library built from source (only
+    where the reference checkout exists)."""
+    ref = oracle.load_reference()
+    if ref is None:
+        pytest.skip("reference library not built here")
+    rng = np.random.default_rng(5)
+    x = rng.uniform(-10, 10, (500, 3)).astype(np.float32)
+    x = x[np.linalg.norm(x, axis=1) > 2.0]
+    q = rng.normal(0, 0.4, len(x)).astype(np.float32)
+    pts = rng.uniform(-1, 1, (64, 3)).astype(np.float32)
+    E = np.zeros_like(pts)
+    ref.compute_looped_field(len(pts), len(q), pts, x, q, E)
+    E32 = oracle.field_grid_f32(pts, x, q)
+    assert np.abs(E32 - E).max() <= 2e-6 * np.abs(E).max()
+    ret = np.zeros(2, np.float32)
+    dims = np.array([1.0, 1.0, 1.0], np.float32)
+    ref.thread_operation(len(q), 200, np.float32(0.01), pts[0].copy(), dims, x, q, ret)
+    r64, _, _ = oracle.topo_lines_f64(pts[:1], [200], x, q, 0.01, dims)
+    assert abs(r64[0, 0] - ret[0]) < 5e-6
