@@ -179,6 +179,10 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-extras", action="store_true", help="skip the FP64 / grid / CPU comparison legs")
+    ap.add_argument("--lines", type=int, default=N_LINES, help="streamlines per step (smaller cases for ncu)")
+    ap.add_argument("--workload", default="topo", choices=["topo", "grid"],
+                    help="grid: the 64-frame batched volume + volume_ESP workload instead")
+    ap.add_argument("--frames", type=int, default=64, help="frames of the grid workload")
     args = ap.parse_args()
     if args.warmup < 3:
         ap.error("--warmup must be >= 3")
@@ -205,7 +209,11 @@ def main():
 
     gbuild.build_library()
     dev = torch.device("cuda", local_rank)
+    if args.workload == "grid":
+        return grid_main(args, rank, world, dev, torch, dist)
     x, q, starts, caps = make_inputs(rank)
+    if args.lines != N_LINES:
+        starts, caps = starts[:args.lines], caps[:args.lines]
     d_x = torch.from_numpy(x).to(dev)
     d_q = torch.from_numpy(q).to(dev)
     d_starts = torch.from_numpy(starts).to(dev)
@@ -257,7 +265,8 @@ def main():
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         total_s = float(t.item())
 
-    value = N_LINES * world * args.steps / total_s
+    n_lines = len(starts)
+    value = n_lines * world * args.steps / total_s
     pe_per_s = pe_step * world * args.steps / total_s
     avg_kern_s = statistics.mean(kern_ms) * 1e-3
     achieved = pe_step * FLOPS_PER_PAIR / avg_kern_s
@@ -266,7 +275,7 @@ def main():
         "warmup": args.warmup, "ms_per_step": 1e3 * total_s / args.steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic (seeded; no dataset ships with the benchmark)",
-        "config": workload_config("fp32c"),
+        "config": dict(workload_config("fp32c"), n_lines=n_lines),
         "pair_evals_per_s": pe_per_s,
         "latency_ms": {"p50": float(np.percentile(step_ms, 50)), "p99": float(np.percentile(step_ms, 99))},
         "roofline": {"bound": "fp32", "achieved": achieved / 1e12, "peak": ffma / 1e12, "unit": "TFLOP/s",
@@ -292,7 +301,7 @@ def main():
             e2e_t.append(time.perf_counter() - t0)
         h2d = h_starts.nbytes + h_caps.nbytes + h_x.nbytes + h_q.nbytes + r.nbytes
         d2h = r.nbytes + c.nbytes + 8 * 42
-        out["e2e"] = {"value": N_LINES / statistics.median(e2e_t), "unit": "streamlines/s",
+        out["e2e"] = {"value": n_lines / statistics.median(e2e_t), "unit": "streamlines/s",
                       "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
                       "path": "cpetgb_topo_lines + cpetgb_topo_hist2d, CPETGB_HOST, pinned buffers"}
         if not args.no_extras and world == 1:
@@ -310,11 +319,77 @@ def main():
         dist.destroy_process_group()
 
 
+def grid_frames(n_frames, seed=2024):
+    """Batched volume workload: N ~ U[3,000, 40,000] charges (cube edge scaled
+    to keep the density), grids of 11^3, 21^3 or 31^3 points at 0.1 A."""
+    from pycpet_gb300.synth import make_frame
+
+    rng = np.random.default_rng(seed)
+    frames = []
+    for f in range(n_frames):
+        n = int(rng.integers(3000, 40001))
+        half = float(rng.choice([0.5, 1.0, 1.5]))
+        g = np.linspace(-half, half, int(round(2 * half / 0.1)) + 1)
+        pts = np.stack(np.meshgrid(g, g, g, indexing="ij"), -1).reshape(-1, 3)
+        fr = make_frame(n, seed=5000 + f)
+        frames.append((pts, fr["x"], fr["q"]))
+    return frames
+
+
+def grid_main(args, rank, world, dev, torch, dist):
+    """--workload grid: field + potential of a frame batch in one descriptor-
+    table launch each (FP32C), device-resident inputs, per-step events."""
+    from pycpet_gb300 import _lib
+    from pycpet_gb300.core import GridBatch
+
+    frames = grid_frames(args.frames, seed=2024 + rank)
+    gbs = [GridBatch(frames, kind=k, precision="fp32c", device=True) for k in ("field", "esp")]
+    stream = torch.cuda.current_stream(dev)
+    flush = torch.empty(L2_FLUSH_BYTES, dtype=torch.uint8, device=dev)
+    for _ in range(args.warmup):
+        for gb in gbs:
+            gb.run()
+    ffma = _lib.measure_peak(0)
+    evs = [[torch.cuda.Event(enable_timing=True) for _ in range(3)] for _ in range(args.steps)]
+    if world > 1:
+        dist.barrier()
+    torch.cuda.synchronize()
+    for k in range(args.steps):
+        evs[k][0].record(stream)
+        gbs[0].run()
+        evs[k][1].record(stream)
+        gbs[1].run()
+        evs[k][2].record(stream)
+        flush.fill_(k & 0xFF)
+    torch.cuda.synchronize()
+    if world > 1:
+        dist.barrier()
+    _lib.check(_lib.lib().cpetgb_synchronize(stream.cuda_stream))
+    f_ms = [e[0].elapsed_time(e[1]) for e in evs]
+    e_ms = [e[1].elapsed_time(e[2]) for e in evs]
+    pe = gbs[0].pair_evals
+    total_s = (sum(f_ms) + sum(e_ms)) * 1e-3
+    out = {"metric": METRIC, "value": 2 * pe * world * args.steps / total_s, "unit": "pair-evals/s",
+           "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+           "ms_per_step": 1e3 * total_s / args.steps, "higher_is_better": True, "scaling": "weak",
+           "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded)",
+           "config": {"workload": f"batched volume + volume_ESP, {args.frames} frames, FP32C",
+                      "pair_evals_per_kind": pe},
+           "field_pair_evals_per_s": pe / (statistics.mean(f_ms) * 1e-3),
+           "esp_pair_evals_per_s": pe / (statistics.mean(e_ms) * 1e-3),
+           "roofline": {"bound": "fp32", "achieved": pe * FLOPS_PER_PAIR / (statistics.mean(f_ms) * 1e-3) / 1e12,
+                        "peak": ffma / 1e12, "unit": "TFLOP/s",
+                        "frac": pe * FLOPS_PER_PAIR / (statistics.mean(f_ms) * 1e-3) / ffma,
+                        "traffic": None, "kernel": "grid_kernel (FP32C field)"}}
+    if rank == 0:
+        print(json.dumps(out), flush=True)
+    if world > 1:
+        dist.destroy_process_group()
+
+
 def extras(d_starts, d_caps, d_x, d_q, torch, topo_lines, GridBatch):
     """FP64 plain form on a subset of the same lines (same subset in FP32C for
     the speed-up), and the batched volume/ESP grid workload in both forms."""
-    from pycpet_gb300.synth import make_frame
-
     n_sub = 16384
     res = {}
     for prec in ("fp32c", "fp64"):
@@ -333,15 +408,7 @@ def extras(d_starts, d_caps, d_x, d_q, torch, topo_lines, GridBatch):
                 "speedup_fp32c_vs_fp64": res["fp64"]["seconds"] / res["fp32c"]["seconds"]}
 
     # batched volume + volume_ESP: 64 frames, N ~ U[3k, 40k], grids 11^3/21^3/31^3
-    rng = np.random.default_rng(2024)
-    frames = []
-    for f in range(64):
-        n = int(rng.integers(3000, 40001))
-        half = float(rng.choice([0.5, 1.0, 1.5]))
-        g = np.linspace(-half, half, int(round(2 * half / 0.1)) + 1)
-        pts = np.stack(np.meshgrid(g, g, g, indexing="ij"), -1).reshape(-1, 3)
-        fr = make_frame(n, seed=5000 + f)
-        frames.append((pts, fr["x"], fr["q"]))
+    frames = grid_frames(64)
     grid = {}
     for kind in ("field", "esp"):
         for prec in ("fp32c", "fp64"):

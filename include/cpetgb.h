@@ -115,6 +115,20 @@ int cpetgb_topo_lines(int precision, int mem, int n_lines, int n_charges, const 
                       const int32_t* n_iter, double step, const double* half_dims,
                       const double* x, const double* q, double* result, double* ends,
                       int32_t* steps, void* stream);
+/* Streamlines for callers that must not have device memory allocated on their
+ * behalf (device memory reserved up front by their own allocator, or a fixed
+ * footprint after start-up).  No counterpart in the reference.  Same arguments
+ * and results as cpetgb_topo_lines with mem = CPETGB_DEVICE (every data pointer
+ * a device pointer, half_dims on the host), but the scratch lives in a fixed
+ * ~512 KiB device array inside the library, so at most 16384 charges (larger
+ * frames return CPETGB_EINVAL).  No cudaMalloc/cudaFree is called.  The first
+ * call on a device looks the array up (cudaGetSymbolAddress): make it before any
+ * stream capture.  The call waits for `stream` and returns the device status.
+ * All calls share the array: calls that overlap on the GPU race. */
+int cpetgb_topo_lines_noalloc(int precision, int n_lines, int n_charges, const double* starts,
+                              const int32_t* n_iter, double step, const double* half_dims,
+                              const double* x, const double* q, double* result, double* ends,
+                              int32_t* steps, void* stream);
 /* 2-D histogram of result[L][2] with numpy.histogram2d's edges and binning.
  * range (HOST) = {dist_lo, dist_hi, curv_lo, curv_hi}; a NaN bound is taken
  * from the data (column min / max).  counts[nb_dist][nb_curv] (uint64) are

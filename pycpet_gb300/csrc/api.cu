@@ -384,6 +384,8 @@ std::vector<double> widen(const float* p, size_t n) {
 
 }  // namespace
 
+int cpetgb::set_error(int code, const char* msg) { return fail(code, "%s", msg); }
+
 extern "C" {
 
 int cpetgb_version(void) { return kVersion; }

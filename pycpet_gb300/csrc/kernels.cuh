@@ -84,6 +84,9 @@ cudaError_t launch_topo(int prec, const TopoParams& p, int num_sms, cudaStream_t
 size_t topo_resident_limit(int prec);  // max charges held resident in shared memory
 int topo_charge_pad();                 // packed charge arrays are padded to this multiple
 
+// api.cu: records `msg` as the calling thread's last error and returns `code`.
+int set_error(int code, const char* msg);
+
 // hist.cu
 cudaError_t launch_hist2d(int n, const double* vals, int nb0, int nb1, const double* range,
                           double* edges, unsigned long long* counts, int* status,
