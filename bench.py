@@ -180,8 +180,11 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-extras", action="store_true", help="skip the FP64 / grid / CPU comparison legs")
     ap.add_argument("--lines", type=int, default=N_LINES, help="streamlines per step (smaller cases for ncu)")
-    ap.add_argument("--workload", default="topo", choices=["topo", "grid"],
-                    help="grid: the 64-frame batched volume + volume_ESP workload instead")
+    ap.add_argument("--workload", default="topo", choices=["topo", "grid", "topo-batch"],
+                    help="grid: the 64-frame batched volume + volume_ESP workload; topo-batch: "
+                         "frames of 5,000-20,000 charges with uneven line counts in one launch")
+    ap.add_argument("--line-scale", type=float, default=0.1,
+                    help="topo-batch: fraction of the 100,000-1,000,000 lines per frame")
     ap.add_argument("--frames", type=int, default=64, help="frames of the grid workload")
     args = ap.parse_args()
     if args.warmup < 3:
@@ -211,6 +214,8 @@ def main():
     dev = torch.device("cuda", local_rank)
     if args.workload == "grid":
         return grid_main(args, rank, world, dev, torch, dist)
+    if args.workload == "topo-batch":
+        return topo_batch_main(args, rank, world, dev, torch, dist)
     x, q, starts, caps = make_inputs(rank)
     if args.lines != N_LINES:
         starts, caps = starts[:args.lines], caps[:args.lines]
@@ -387,42 +392,133 @@ def grid_main(args, rank, world, dev, torch, dist):
         dist.destroy_process_group()
 
 
+def topo_batch_main(args, rank, world, dev, torch, dist):
+    """--workload topo-batch: frames of 5,000-20,000 charges (density kept),
+    100,000-1,000,000 lines per frame scaled by --line-scale, half-width 1.5 A,
+    step 0.001 A, cap 6,000; all frames in one persistent launch (FP32C)."""
+    from pycpet_gb300 import _lib
+    from pycpet_gb300.core import TopoBatch
+    from pycpet_gb300.synth import make_frame, random_start_points
+
+    rng = np.random.default_rng(3030 + rank)
+    n_frames = args.frames if args.frames != 64 else 32
+    frames = []
+    for f in range(n_frames):
+        n = int(rng.integers(5000, 20001))
+        L = max(1, int(rng.integers(100_000, 1_000_001) * args.line_scale))
+        fr = make_frame(n, seed=7000 + f + 100 * rank)
+        frames.append({"x": fr["x"], "q": fr["q"], "starts": random_start_points(L, [HALF] * 3, 8000 + f),
+                       "n_iter": CAP, "step": STEP, "half_dims": [HALF] * 3})
+    tb = TopoBatch(frames, precision="fp32c", device=True)
+    res, steps = tb.run(return_steps=True)
+    torch.cuda.synchronize()
+    steps = steps.cpu().numpy()
+    pe = sum(pair_evals(s, len(fr["q"])) for fr, s in zip(frames, tb.split(steps)))
+    for _ in range(args.warmup - 1):
+        tb.run()
+    stream = torch.cuda.current_stream(dev)
+    evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    if world > 1:
+        dist.barrier()
+    torch.cuda.synchronize()
+    for e0, e1 in evs:
+        e0.record(stream)
+        tb.run()
+        e1.record(stream)
+    torch.cuda.synchronize()
+    if world > 1:
+        dist.barrier()
+    _lib.check(_lib.lib().cpetgb_synchronize(stream.cuda_stream))
+    ms = [a.elapsed_time(b) for a, b in evs]
+    total_s = sum(ms) * 1e-3
+    out = {"metric": METRIC, "value": tb.n_lines * world * args.steps / total_s, "unit": "streamlines/s",
+           "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * total_s / args.steps,
+           "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+           "data": "synthetic (seeded)",
+           "config": {"workload": f"batched topo, {n_frames} frames of 5,000-20,000 charges, "
+                                  f"{args.line_scale:g} x (100,000-1,000,000) lines per frame, one launch",
+                      "n_lines": tb.n_lines, "precision": "fp32c"},
+           "pair_evals_per_s": pe * world * args.steps / total_s,
+           "latency_ms": {"p50": float(np.percentile(ms, 50)), "p99": float(np.percentile(ms, 99))}}
+    if rank == 0:
+        print(json.dumps(out), flush=True)
+    if world > 1:
+        dist.destroy_process_group()
+
+
 def extras(d_starts, d_caps, d_x, d_q, torch, topo_lines, GridBatch):
     """FP64 plain form on a subset of the same lines (same subset in FP32C for
     the speed-up), and the batched volume/ESP grid workload in both forms."""
+    from pycpet_gb300 import topo_hist2d
+
     n_sub = 16384
-    res = {}
+    res, outs = {}, {}
     for prec in ("fp32c", "fp64"):
-        topo_lines(d_starts[:n_sub], d_caps[:n_sub], d_x, d_q, STEP, [HALF] * 3, precision=prec)
+        topo_lines(d_starts[:1024], d_caps[:1024], d_x, d_q, STEP, [HALF] * 3, precision=prec)
         torch.cuda.synchronize()
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         e0.record()
-        _, steps = topo_lines(d_starts[:n_sub], d_caps[:n_sub], d_x, d_q, STEP, [HALF] * 3, precision=prec,
-                              return_steps=True)
+        r, ends, steps = topo_lines(d_starts[:n_sub], d_caps[:n_sub], d_x, d_q, STEP, [HALF] * 3,
+                                    precision=prec, return_ends=True, return_steps=True)
         e1.record()
         torch.cuda.synchronize()
         s = e0.elapsed_time(e1) * 1e-3
+        outs[prec] = (r.cpu().numpy(), ends.cpu().numpy(), steps.cpu().numpy())
         res[prec] = {"streamlines_per_s": n_sub / s,
-                     "pair_evals_per_s": pair_evals(steps.cpu().numpy(), N_CHARGES) / s, "seconds": s}
+                     "pair_evals_per_s": pair_evals(outs[prec][2], N_CHARGES) / s, "seconds": s}
+    (r32, e32, s32), (r64, e64, s64) = outs["fp32c"], outs["fp64"]
+    cmax = float(np.nanmax(r64[:, 1]))
+    h32 = topo_hist2d(r32, bins=(20, 20), range=((0.0, 5.2), (0.0, cmax))).astype(np.float64)
+    h64 = topo_hist2d(r64, bins=(20, 20), range=((0.0, 5.2), (0.0, cmax))).astype(np.float64)
+    end_err = np.linalg.norm(e32 - e64, axis=1)
+    curv_rel = np.abs(r32[:, 1] - r64[:, 1]) / np.maximum(np.abs(r64[:, 1]), 1e-300)
     topo_cmp = {"sample": f"first {n_sub} lines", "fp32c": res["fp32c"], "fp64": res["fp64"],
-                "speedup_fp32c_vs_fp64": res["fp64"]["seconds"] / res["fp32c"]["seconds"]}
+                "speedup_fp32c_vs_fp64": res["fp64"]["seconds"] / res["fp32c"]["seconds"],
+                "error_fp32c_vs_fp64": {
+                    "endpoint_A": {"p50": float(np.median(end_err)), "p99": float(np.quantile(end_err, 0.99)),
+                                   "max": float(end_err.max())},
+                    "distance_A_max": float(np.abs(r32[:, 0] - r64[:, 0]).max()),
+                    "curvature_rel": {"p50": float(np.median(curv_rel)), "p99": float(np.quantile(curv_rel, 0.99)),
+                                      "max": float(curv_rel.max())},
+                    "step_count_mismatch_frac": float(np.mean(s32 != s64)),
+                    "histogram_L1": float(np.abs(h32 / h32.sum() - h64 / h64.sum()).sum()),
+                    "histogram_range": [[0.0, 5.2], [0.0, cmax]]}}
 
     # batched volume + volume_ESP: 64 frames, N ~ U[3k, 40k], grids 11^3/21^3/31^3
     frames = grid_frames(64)
     grid = {}
     for kind in ("field", "esp"):
+        vals = {}
         for prec in ("fp32c", "fp64"):
             gb = GridBatch(frames, kind=kind, precision=prec, device=True)
             gb.run()
             torch.cuda.synchronize()
             e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
             e0.record()
-            gb.run()
+            out = gb.run()
             e1.record()
             torch.cuda.synchronize()
             s = e0.elapsed_time(e1) * 1e-3
             grid[f"{kind}_{prec}"] = {"pair_evals_per_s": gb.pair_evals / s, "ms": s * 1e3}
+            vals[prec] = [o.copy() for o in gb.split(out.cpu().numpy())]
             del gb
+        # FP32C error against the FP64 form (itself within 1e-11 of the CPU FP64 oracle), per frame
+        worst_rel, worst_norm, rels = 0.0, 0.0, []
+        for a, b in zip(vals["fp32c"], vals["fp64"]):
+            nb = np.linalg.norm(b, axis=1)
+            err = np.linalg.norm(a - b, axis=1)
+            mask = nb >= 1e-6 * np.median(nb)          # tiny |ref| points are flagged, not scored
+            rel = err[mask] / nb[mask]
+            rels.append(rel)
+            worst_rel = max(worst_rel, float(rel.max()))
+            worst_norm = max(worst_norm, float(err.max() / nb.max()))
+        rels = np.concatenate(rels)
+        grid[f"{kind}_fp32c_error"] = {
+            "max_rel_per_point": worst_rel, "p999_rel_per_point": float(np.quantile(rels, 0.999)),
+            "frac_points_above_1e-5": float(np.mean(rels > 1e-5)),
+            "max_normwise_rel": worst_norm, "frames": len(frames), "points": int(rels.size),
+            "rule": "per point |dE|/|E_ref| (points with |E_ref| < 1e-6 * frame median flagged); normwise "
+                    "= max|dE| / max|E_ref| per frame; reference = the FP64 form"}
     grid["workload"] = "64 frames, 3,000-40,000 charges, 11^3/21^3/31^3 grids, one descriptor-table launch"
     grid["pair_evals"] = int(sum(len(p) * len(qq) for p, _, qq in frames))
     return {"topo_fp64_vs_fp32c": topo_cmp, "grid_batch": grid}

@@ -115,6 +115,15 @@ int cpetgb_topo_lines(int precision, int mem, int n_lines, int n_charges, const 
                       const int32_t* n_iter, double step, const double* half_dims,
                       const double* x, const double* q, double* result, double* ends,
                       int32_t* steps, void* stream);
+/* Streamlines of many frames in one persistent launch.  desc is a HOST array
+ * [n_frames][4] of int64 {charge_offset, n_charges, line_offset, n_lines} into
+ * x/q and starts/n_iter/result/ends/steps; params is a HOST array
+ * [n_frames][4] of double {step, half_x, half_y, half_z}.  Frames are worked
+ * in table order; results as cpetgb_topo_lines, at each line's index. */
+int cpetgb_topo_batch(int precision, int mem, int n_frames, const int64_t* desc,
+                      const double* params, const double* starts, const int32_t* n_iter,
+                      const double* x, const double* q, double* result, double* ends,
+                      int32_t* steps, void* stream);
 /* Streamlines for callers that must not have device memory allocated on their
  * behalf (device memory reserved up front by their own allocator, or a fixed
  * footprint after start-up).  No counterpart in the reference.  Same arguments

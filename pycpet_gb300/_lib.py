@@ -48,6 +48,7 @@ SIGNATURES = {
     "cpetgb_esp_grid": [_i, _i, _i, _i, _vp, _vp, _vp, _vp, _vp],
     "cpetgb_grid_batch": [_i, _i, _i, _i, _i, _vp, _vp, _vp, _vp, _vp, _vp],
     "cpetgb_topo_lines": [_i, _i, _i, _i, _vp, _vp, _d, _vp, _vp, _vp, _vp, _vp, _vp, _vp],
+    "cpetgb_topo_batch": [_i, _i, _i, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp],
     "cpetgb_topo_lines_noalloc": [_i, _i, _i, _vp, _vp, _d, _vp, _vp, _vp, _vp, _vp, _vp, _vp],
     "cpetgb_topo_hist2d": [_i, _i, _vp, _i, _i, _vp, _vp, _vp, _vp],
 }

@@ -236,6 +236,73 @@ def topo_lines(starts, n_iter, x, q, step, half_dims, precision="fp32c", return_
     return out[0] if len(out) == 1 else tuple(out)
 
 
+class TopoBatch:
+    """Streamlines of many frames in one persistent launch (frame descriptor table).
+
+    frames: sequence of dicts with keys starts (L_f,3), n_iter (L_f,) or scalar,
+    x (N_f,3), q (N_f,), step, half_dims (3,).  Inputs are concatenated once;
+    ``run()`` returns (L_total, 2) results (split per frame with ``split``).
+    With ``device=True`` the inputs live in torch CUDA tensors.
+    """
+
+    def __init__(self, frames, precision="fp32c", device=False):
+        self.prec = precision_code(precision)
+        starts, caps, xs, qs, desc, params = [], [], [], [], [], []
+        lo = co = 0
+        for fr in frames:
+            st = np.asarray(fr["starts"], np.float64).reshape(-1, 3)
+            L = len(st)
+            it = np.broadcast_to(np.asarray(fr["n_iter"]), (L,)).astype(np.int32)
+            x = np.asarray(fr["x"], np.float64).reshape(-1, 3)
+            q = np.asarray(fr["q"], np.float64).reshape(-1)
+            h = np.asarray(fr["half_dims"], np.float64).reshape(3)
+            desc.append((co, len(q), lo, L))
+            params.append((float(fr["step"]), h[0], h[1], h[2]))
+            starts.append(st), caps.append(it), xs.append(x), qs.append(q)
+            lo += L
+            co += len(q)
+        self.desc = np.ascontiguousarray(np.array(desc, dtype=np.int64).reshape(-1, 4))
+        self.params = np.ascontiguousarray(np.array(params, dtype=np.float64).reshape(-1, 4))
+        self.starts = np.ascontiguousarray(np.concatenate(starts) if starts else np.zeros((0, 3)))
+        self.n_iter = np.ascontiguousarray(np.concatenate(caps) if caps else np.zeros(0, np.int32))
+        self.x = np.ascontiguousarray(np.concatenate(xs) if xs else np.zeros((0, 3)))
+        self.q = np.ascontiguousarray(np.concatenate(qs) if qs else np.zeros(0))
+        self.n_lines = lo
+        self.device = device
+        if device:
+            import torch
+
+            self.starts = torch.from_numpy(self.starts).cuda()
+            self.n_iter = torch.from_numpy(self.n_iter).cuda()
+            self.x = torch.from_numpy(self.x).cuda()
+            self.q = torch.from_numpy(self.q).cuda()
+
+    def run(self, return_steps=False):
+        if self.device:
+            import torch
+
+            dev = self.starts.device
+            res = torch.empty((self.n_lines, 2), dtype=torch.float64, device=dev)
+            steps = torch.empty((self.n_lines,), dtype=torch.int32, device=dev) if return_steps else None
+            with torch.cuda.device(dev):
+                check(lib().cpetgb_topo_batch(self.prec, DEVICE, len(self.desc), self.desc.ctypes.data,
+                                              self.params.ctypes.data, self.starts.data_ptr(),
+                                              self.n_iter.data_ptr(), self.x.data_ptr(), self.q.data_ptr(),
+                                              res.data_ptr(), None, steps.data_ptr() if steps is not None else None,
+                                              _stream_of(self.starts)))
+        else:
+            res = np.empty((self.n_lines, 2))
+            steps = np.empty(self.n_lines, dtype=np.int32) if return_steps else None
+            check(lib().cpetgb_topo_batch(self.prec, HOST, len(self.desc), self.desc.ctypes.data,
+                                          self.params.ctypes.data, self.starts.ctypes.data, self.n_iter.ctypes.data,
+                                          self.x.ctypes.data, self.q.ctypes.data, res.ctypes.data, None,
+                                          steps.ctypes.data if steps is not None else None, None))
+        return (res, steps) if return_steps else res
+
+    def split(self, out):
+        return [out[lo:lo + L] for _, _, lo, L in self.desc]
+
+
 def topo_hist2d(result, bins=(20, 20), range=((0.0, 5.2), (0.0, None)), return_edges=False):
     """2-D histogram of (distance, curvature) rows with numpy.histogram2d's
     edges and binning (CPET/utils/calculator.py:702-707).  A range bound of

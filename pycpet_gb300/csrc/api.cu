@@ -148,7 +148,8 @@ int finish(Ctx* c, cudaStream_t s) {
 
 bool valid_prec(int p) { return p == CPETGB_FP64 || p == CPETGB_FP32C; }
 bool valid_mem(int m) { return m == CPETGB_HOST || m == CPETGB_DEVICE; }
-size_t packed_size(int prec) { return prec == CPETGB_FP32C ? 16 : 32; }
+size_t packed_size(int prec) { return prec == CPETGB_FP32C ? 16 : 32; }  // streamline layouts
+constexpr size_t kGridRecord = 32;  // grid layouts: Charge64 or the duplicated FP32C record
 
 // ---------------------------------------------------------------------------
 // Grid work decomposition.
@@ -245,7 +246,7 @@ int grid_batch_impl(int kind, int prec, int mem, int clamp, int n_frames, const 
   GridItem* d_items = nullptr;
   GridFinal* d_fin = nullptr;
   double* partial = nullptr;
-  CK(S.get(&packed, size_t(std::max<int64_t>(tot_ch, 1)) * packed_size(prec)), "alloc packed charges");
+  CK(S.get(&packed, size_t(std::max<int64_t>(tot_ch, 1)) * kGridRecord), "alloc packed charges");
   CK(h2d(&d_items, S, plan.items.data(), plan.items.size()), "copy work items");
   if (!plan.finals.empty()) {
     CK(h2d(&d_fin, S, plan.finals.data(), plan.finals.size()), "copy split table");
@@ -303,7 +304,7 @@ int topo_impl(int prec, int mem, int L, int N, const double* starts, const int32
     if (ends) CK(S.get(&dends, size_t(L) * 3), "alloc ends");
     if (steps) CK(S.get(&dsteps, size_t(L)), "alloc steps");
   }
-  const int pad = topo_charge_pad();
+  const int pad = topo_charge_pad(prec);
   const int64_t n_pad = ((std::max(N, 1) + int64_t(pad) - 1) / pad) * pad;
   unsigned char* packed = nullptr;
   int* queue = nullptr;
@@ -312,7 +313,7 @@ int topo_impl(int prec, int mem, int L, int N, const double* starts, const int32
   CK(cudaMemsetAsync(queue, 0, sizeof(int), s), "zero queue");
   if (reinterpret_cast<uintptr_t>(packed) % 16 != 0)
     return fail(CPETGB_ECUDA, "scratch allocation is not 16-byte aligned");
-  CK(launch_pack_charges(prec, N, n_pad, dx, dq, packed, s), "pack charges");
+  CK(launch_pack_topo(prec, N, n_pad, dx, dq, packed, s), "pack charges");
   TopoParams p;
   p.n_lines = L;
   p.n_charges = N;
@@ -335,6 +336,113 @@ int topo_impl(int prec, int mem, int L, int N, const double* starts, const int32
          "copy ends");
     if (steps)
       CK(cudaMemcpyAsync(steps, dsteps, size_t(L) * sizeof(int32_t), cudaMemcpyDeviceToHost, s),
+         "copy steps");
+    return finish(c, s);
+  }
+  return CPETGB_OK;
+}
+
+int topo_batch_impl(int prec, int mem, int F, const int64_t* desc, const double* params,
+                    const double* starts, const int32_t* n_iter, const double* x, const double* q,
+                    double* result, double* ends, int32_t* steps, void* stream) {
+  if (!valid_prec(prec)) return fail(CPETGB_EINVAL, "bad precision %d", prec);
+  if (!valid_mem(mem)) return fail(CPETGB_EINVAL, "bad memory kind %d", mem);
+  if (F < 0 || (F > 0 && (!desc || !params))) return fail(CPETGB_EINVAL, "bad frame table");
+  const int pad = topo_charge_pad(prec);
+  const size_t res_limit = prec == CPETGB_FP32C ? topo_resident_limit(prec) : 0;
+  std::vector<TopoFrame> frames(F);
+  std::vector<int64_t> src(2 * size_t(F));
+  int64_t tot_lines = 0, tot_ch = 0, packed_elems = 0;
+  int max_res = 0, max_pairs = 0;
+  for (int f = 0; f < F; ++f) {
+    const int64_t co = desc[4 * f], n = desc[4 * f + 1], lo = desc[4 * f + 2], L = desc[4 * f + 3];
+    if (co < 0 || n < 0 || lo < 0 || L < 0 || n > INT_MAX / 2 || L > INT_MAX)
+      return fail(CPETGB_EINVAL, "frame %d: negative or oversized offset/count", f);
+    const double* pr = params + 4 * f;
+    if (!std::isfinite(pr[0])) return fail(CPETGB_EINVAL, "frame %d: step must be finite", f);
+    for (int k = 1; k < 4; ++k)
+      if (!std::isfinite(pr[k]) || pr[k] < 0)
+        return fail(CPETGB_EINVAL, "frame %d: half-widths must be finite and >= 0", f);
+    TopoFrame& fr = frames[f];
+    fr.n_pad = static_cast<int32_t>(((std::max<int64_t>(n, 1) + pad - 1) / pad) * pad);
+    fr.packed_off = packed_elems;
+    // FP32C frames occupy n_pad float4 (pair block A then B); FP64 n_pad Charge64
+    packed_elems += fr.n_pad;
+    fr.line_off = lo;
+    fr.n_lines = static_cast<int32_t>(L);
+    fr.resident = (prec == CPETGB_FP32C && static_cast<size_t>(fr.n_pad) <= res_limit) ? 1 : 0;
+    fr.pad_ = 0;
+    fr.step = pr[0];
+    for (int k = 0; k < 3; ++k) fr.half[k] = pr[1 + k];
+    if (fr.resident) max_res = std::max(max_res, int(fr.n_pad));
+    max_pairs = std::max(max_pairs, int(fr.n_pad));
+    src[2 * f] = co;
+    src[2 * f + 1] = n;
+    tot_lines = std::max(tot_lines, lo + L);
+    tot_ch = std::max(tot_ch, co + n);
+  }
+  if (tot_lines > INT_MAX) return fail(CPETGB_EINVAL, "too many lines");
+  if (tot_lines == 0) return CPETGB_OK;
+  if (!starts || !n_iter || !result) return fail(CPETGB_EINVAL, "line pointer is NULL");
+  if (tot_ch > 0 && (!x || !q)) return fail(CPETGB_EINVAL, "charge pointer is NULL");
+  int rc;
+  Ctx* c = context(&rc);
+  if (!c) return rc;
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  if (mem == CPETGB_HOST && !s) s = c->stream;
+  const size_t L = size_t(tot_lines);
+  Scratch S(s);
+  const double *ds = starts, *dx = x, *dq = q;
+  const int32_t* dn = n_iter;
+  double *dres = result, *dends = ends;
+  int32_t* dsteps = steps;
+  if (mem == CPETGB_HOST) {
+    CK(h2d(const_cast<double**>(&ds), S, starts, L * 3), "copy starts");
+    CK(h2d(const_cast<int32_t**>(&dn), S, n_iter, L), "copy n_iter");
+    if (tot_ch) {
+      CK(h2d(const_cast<double**>(&dx), S, x, size_t(tot_ch) * 3), "copy charge positions");
+      CK(h2d(const_cast<double**>(&dq), S, q, size_t(tot_ch)), "copy charges");
+    }
+    CK(S.get(&dres, L * 2), "alloc result");
+    if (ends) CK(S.get(&dends, L * 3), "alloc ends");
+    if (steps) CK(S.get(&dsteps, L), "alloc steps");
+  }
+  unsigned char* packed = nullptr;
+  TopoFrame* d_frames = nullptr;
+  int64_t* d_src = nullptr;
+  int* queues = nullptr;
+  CK(S.get(&packed, size_t(std::max<int64_t>(packed_elems, 1)) * packed_size(prec)),
+     "alloc packed charges");
+  if (reinterpret_cast<uintptr_t>(packed) % 16 != 0)
+    return fail(CPETGB_ECUDA, "scratch allocation is not 16-byte aligned");
+  CK(h2d(&d_frames, S, frames.data(), frames.size()), "copy frame table");
+  CK(h2d(&d_src, S, src.data(), src.size()), "copy frame sources");
+  CK(S.get(&queues, size_t(F)), "alloc queues");
+  CK(cudaMemsetAsync(queues, 0, sizeof(int) * size_t(F), s), "zero queues");
+  CK(launch_pack_topo_frames(prec, F, d_frames, d_src, dx, dq, packed, max_pairs, s),
+     "pack charges");
+  TopoParams p{};
+  p.n_lines = static_cast<int>(tot_lines);
+  p.starts = ds;
+  p.n_iter = dn;
+  p.packed = packed;
+  p.result = dres;
+  p.ends = dends;
+  p.steps = dsteps;
+  p.queue = queues;
+  p.status = c->status;
+  p.frames = d_frames;
+  p.n_frames = F;
+  p.max_resident_pad = max_res;
+  CK(launch_topo_frames(prec, p, c->sms, s), "topo kernel launch");
+  if (mem == CPETGB_HOST) {
+    CK(cudaMemcpyAsync(result, dres, L * 2 * sizeof(double), cudaMemcpyDeviceToHost, s),
+       "copy result");
+    if (ends)
+      CK(cudaMemcpyAsync(ends, dends, L * 3 * sizeof(double), cudaMemcpyDeviceToHost, s),
+         "copy ends");
+    if (steps)
+      CK(cudaMemcpyAsync(steps, dsteps, L * sizeof(int32_t), cudaMemcpyDeviceToHost, s),
          "copy steps");
     return finish(c, s);
   }
@@ -443,6 +551,14 @@ int cpetgb_topo_lines(int precision, int mem, int n_lines, int n_charges, const 
                       int32_t* steps, void* stream) {
   return topo_impl(precision, mem, n_lines, n_charges, starts, n_iter, step, half_dims, x, q,
                    result, ends, steps, stream);
+}
+
+int cpetgb_topo_batch(int precision, int mem, int n_frames, const int64_t* desc,
+                      const double* params, const double* starts, const int32_t* n_iter,
+                      const double* x, const double* q, double* result, double* ends,
+                      int32_t* steps, void* stream) {
+  return topo_batch_impl(precision, mem, n_frames, desc, params, starts, n_iter, x, q, result, ends,
+                         steps, stream);
 }
 
 int cpetgb_topo_hist2d(int mem, int n_lines, const double* result, int nb_dist, int nb_curv,

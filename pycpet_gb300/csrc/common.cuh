@@ -96,6 +96,39 @@ __device__ __forceinline__ float rsqrt_mufu(float x) {
   return y;
 }
 
+// Packed FP32x2 arithmetic (two IEEE binary32 lanes in one 64-bit register
+// pair; sm_100+).  One instruction issues two FP32 operations, which halves the
+// issue slots of the pair loops; the FP32 pipe throughput itself is unchanged.
+__device__ __forceinline__ uint64_t pk2(float lo, float hi) {
+  uint64_t r;
+  asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(lo), "f"(hi));
+  return r;
+}
+__device__ __forceinline__ void upk2(uint64_t v, float& lo, float& hi) {
+  asm("mov.b64 {%0, %1}, %2;" : "=f"(lo), "=f"(hi) : "l"(v));
+}
+__device__ __forceinline__ uint64_t sub2(uint64_t a, uint64_t b) {
+  uint64_t d;
+  asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+  return d;
+}
+__device__ __forceinline__ uint64_t mul2(uint64_t a, uint64_t b) {
+  uint64_t d;
+  asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+  return d;
+}
+__device__ __forceinline__ uint64_t fma2(uint64_t a, uint64_t b, uint64_t c) {
+  uint64_t d;
+  asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(d) : "l"(a), "l"(b), "l"(c));
+  return d;
+}
+// MUFU rsqrt of both lanes.
+__device__ __forceinline__ uint64_t rsqrt2(uint64_t v) {
+  float a, b;
+  upk2(v, a, b);
+  return pk2(rsqrt_mufu(a), rsqrt_mufu(b));
+}
+
 // Kahan (1965) compensated accumulation of t into (s, c); the true sum is s - c.
 __device__ __forceinline__ void kahan_add(float& s, float& c, float t) {
   const float y = __fsub_rn(t, c);

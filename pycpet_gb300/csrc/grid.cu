@@ -33,11 +33,18 @@ constexpr int kStages = 4;
 
 template <int PREC>
 struct GridCfg;
+// FP32C charge record with every component duplicated, {x,x,y,y} {z,z,q,q}:
+// one broadcast 16-byte shared load yields two ready f32x2 operands, and a
+// packed instruction then evaluates the pair term for two grid points.
+struct alignas(32) ChargeDup {
+  ulonglong2 xy;
+  ulonglong2 zq;
+};
 template <>
 struct GridCfg<kFP32C> {
-  using ChargeT = float4;
+  using ChargeT = ChargeDup;
   using Real = float;
-  static constexpr int kTile = 512;  // charges per stage (8 KiB)
+  static constexpr int kTile = 256;  // charges per stage (8 KiB)
 };
 template <>
 struct GridCfg<kFP64> {
@@ -47,8 +54,72 @@ struct GridCfg<kFP64> {
 };
 
 __device__ __forceinline__ double rsqrt_f64(double x) { return rsqrt(x); }
-__device__ __forceinline__ float charge_q(const float4& c) { return c.w; }
 __device__ __forceinline__ double charge_q(const Charge64& c) { return c.q; }
+// {v, v} as one packed 64-bit value.
+__device__ __forceinline__ uint64_t dup2(float v) {
+  const uint64_t b = __float_as_uint(v);
+  return b | (b << 32);
+}
+
+__device__ __forceinline__ uint64_t add2(uint64_t a, uint64_t b) {
+  uint64_t d;
+  asm("add.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+  return d;
+}
+// Kahan accumulation on both lanes of packed pairs.
+__device__ __forceinline__ void kahan_add2(uint64_t& s, uint64_t& c, uint64_t t) {
+  const uint64_t y = sub2(t, c);
+  const uint64_t u = add2(s, y);
+  c = sub2(sub2(u, s), y);
+  s = u;
+}
+
+constexpr int kKahanRun = 16;  // FP32C: charges summed plainly between Kahan steps
+
+// FP32C body: this thread's 4 points as two packed pairs (points k = 2g, 2g+1).
+template <int KIND, bool CLAMP>
+__device__ __forceinline__ void grid_tile_f32x2(const ChargeDup* __restrict__ tl, int cnt,
+                                                const uint64_t (&px)[2], const uint64_t (&py)[2],
+                                                const uint64_t (&pz)[2], uint64_t (&acc)[3][2],
+                                                uint64_t (&cmp)[3][2]) {
+  constexpr int NC = (KIND == kField) ? 3 : 1;
+  for (int j0 = 0; j0 < cnt; j0 += kKahanRun) {
+    const int j1 = min(cnt, j0 + kKahanRun);
+    uint64_t part[NC][2];
+#pragma unroll
+    for (int c = 0; c < NC; ++c) part[c][0] = part[c][1] = 0ull;
+#pragma unroll 4
+    for (int j = j0; j < j1; ++j) {
+      const ulonglong2 xy = tl[j].xy;
+      const ulonglong2 zq = tl[j].zq;
+#pragma unroll
+      for (int g = 0; g < 2; ++g) {
+        const uint64_t dx = sub2(px[g], xy.x);
+        const uint64_t dy = sub2(py[g], xy.y);
+        const uint64_t dz = sub2(pz[g], zq.x);
+        uint64_t r2 = fma2(dx, dx, fma2(dy, dy, mul2(dz, dz)));
+        if constexpr (CLAMP) {  // compute_looped_field's fmaxf(r^2, 1e-6f)
+          float a, b;
+          upk2(r2, a, b);
+          r2 = pk2(fmaxf(a, 1e-6f), fmaxf(b, 1e-6f));
+        }
+        const uint64_t ri = rsqrt2(r2);
+        if constexpr (KIND == kField) {
+          const uint64_t w = mul2(mul2(zq.y, ri), mul2(ri, ri));
+          part[0][g] = fma2(w, dx, part[0][g]);
+          part[1][g] = fma2(w, dy, part[1][g]);
+          part[2][g] = fma2(w, dz, part[2][g]);
+        } else {
+          part[0][g] = fma2(zq.y, ri, part[0][g]);
+        }
+      }
+    }
+#pragma unroll
+    for (int c = 0; c < NC; ++c)
+#pragma unroll
+      for (int g = 0; g < 2; ++g) kahan_add2(acc[c][g], cmp[c][g], part[c][g]);
+  }
+}
 
 template <int PREC, int KIND, bool CLAMP>
 __global__ void __launch_bounds__(kGridThreads)
@@ -87,7 +158,7 @@ __global__ void __launch_bounds__(kGridThreads)
     for (int t = 0; t < min(kStages, n_tiles); ++t) issue(t);
   }
 
-  // This thread's points, in registers.
+  // This thread's points, in registers (FP32C: packed in pairs).
   Real px[kGridPPT], py[kGridPPT], pz[kGridPPT];
 #pragma unroll
   for (int k = 0; k < kGridPPT; ++k) {
@@ -101,13 +172,24 @@ __global__ void __launch_bounds__(kGridThreads)
       px[k] = py[k] = pz[k] = static_cast<Real>(1.0e4);  // far away, never written
     }
   }
+  [[maybe_unused]] uint64_t px2[2], py2[2], pz2[2], acc2[3][2], cmp2[3][2];
+  if constexpr (PREC == kFP32C) {
+#pragma unroll
+    for (int g = 0; g < 2; ++g) {
+      px2[g] = pk2(px[2 * g], px[2 * g + 1]);
+      py2[g] = pk2(py[2 * g], py[2 * g + 1]);
+      pz2[g] = pk2(pz[2 * g], pz[2 * g + 1]);
+#pragma unroll
+      for (int c = 0; c < 3; ++c) acc2[c][g] = cmp2[c][g] = 0ull;
+    }
+  }
 
-  // Running sums: acc = sum, cmp = Kahan compensation (FP32C only).
-  Real acc[NC][kGridPPT], cmp[NC][kGridPPT];
+  // FP64 running sums.
+  Real acc[NC][kGridPPT];
 #pragma unroll
   for (int c = 0; c < NC; ++c)
 #pragma unroll
-    for (int k = 0; k < kGridPPT; ++k) acc[c][k] = cmp[c][k] = Real(0);
+    for (int k = 0; k < kGridPPT; ++k) acc[c][k] = Real(0);
 
   bool ok = true;
   for (int t = 0; t < n_tiles; ++t) {
@@ -119,46 +201,40 @@ __global__ void __launch_bounds__(kGridThreads)
 
     const int cnt = min(TC, n - t * TC);
     const ChargeT* tl = &tile[s][0];
-    Real part[NC][kGridPPT];
+    if constexpr (PREC == kFP32C) {
+      grid_tile_f32x2<KIND, CLAMP>(tl, cnt, px2, py2, pz2, acc2, cmp2);
+    } else {
+      Real part[NC][kGridPPT];
 #pragma unroll
-    for (int c = 0; c < NC; ++c)
+      for (int c = 0; c < NC; ++c)
 #pragma unroll
-      for (int k = 0; k < kGridPPT; ++k) part[c][k] = Real(0);
-
+        for (int k = 0; k < kGridPPT; ++k) part[c][k] = Real(0);
 #pragma unroll 4
-    for (int j = 0; j < cnt; ++j) {
-      const ChargeT ch = tl[j];
+      for (int j = 0; j < cnt; ++j) {
+        const ChargeT ch = tl[j];
 #pragma unroll
-      for (int k = 0; k < kGridPPT; ++k) {
-        const Real dx = px[k] - ch.x;
-        const Real dy = py[k] - ch.y;
-        const Real dz = pz[k] - ch.z;
-        Real r2 = dx * dx + dy * dy + dz * dz;
-        if constexpr (CLAMP) r2 = fmax(r2, Real(1e-6));  // compute_looped_field's fmaxf
-        Real ri;
-        if constexpr (PREC == kFP32C)
-          ri = rsqrt_mufu(r2);
-        else
-          ri = rsqrt_f64(r2);
-        if constexpr (KIND == kField) {
-          const Real w = (charge_q(ch) * ri) * (ri * ri);
-          part[0][k] += w * dx;
-          part[1][k] += w * dy;
-          part[2][k] += w * dz;
-        } else {
-          part[0][k] += charge_q(ch) * ri;
+        for (int k = 0; k < kGridPPT; ++k) {
+          const Real dx = px[k] - ch.x;
+          const Real dy = py[k] - ch.y;
+          const Real dz = pz[k] - ch.z;
+          Real r2 = dx * dx + dy * dy + dz * dz;
+          if constexpr (CLAMP) r2 = fmax(r2, Real(1e-6));  // compute_looped_field's fmaxf
+          const Real ri = rsqrt_f64(r2);
+          if constexpr (KIND == kField) {
+            const Real w = (charge_q(ch) * ri) * (ri * ri);
+            part[0][k] += w * dx;
+            part[1][k] += w * dy;
+            part[2][k] += w * dz;
+          } else {
+            part[0][k] += charge_q(ch) * ri;
+          }
         }
       }
+#pragma unroll
+      for (int c = 0; c < NC; ++c)
+#pragma unroll
+        for (int k = 0; k < kGridPPT; ++k) acc[c][k] += part[c][k];
     }
-#pragma unroll
-    for (int c = 0; c < NC; ++c)
-#pragma unroll
-      for (int k = 0; k < kGridPPT; ++k) {
-        if constexpr (PREC == kFP32C)
-          kahan_add(acc[c][k], cmp[c][k], part[c][k]);
-        else
-          acc[c][k] += part[c][k];
-      }
   }
   if (!ok) return;
 
@@ -168,8 +244,16 @@ __global__ void __launch_bounds__(kGridThreads)
     if (pl >= it.p_count) continue;
 #pragma unroll
     for (int c = 0; c < NC; ++c) {
-      const double v =
-          (static_cast<double>(acc[c][k]) - static_cast<double>(cmp[c][k])) * kCoulomb;
+      double v;
+      if constexpr (PREC == kFP32C) {
+        float sl, sh, cl, ch;
+        upk2(acc2[c][k / 2], sl, sh);
+        upk2(cmp2[c][k / 2], cl, ch);
+        const float sv = (k & 1) ? sh : sl, cv = (k & 1) ? ch : cl;
+        v = (static_cast<double>(sv) - static_cast<double>(cv)) * kCoulomb;
+      } else {
+        v = static_cast<double>(acc[c][k]) * kCoulomb;
+      }
       if (it.slot < 0) {
         out[NC * (it.point_off + it.p_begin + pl) + c] = v;
       } else {
@@ -193,13 +277,22 @@ __global__ void grid_final_kernel(const GridFinal* __restrict__ fin,
   }
 }
 
-__global__ void pack_f32_kernel(int64_t n, int64_t n_pad, const double* __restrict__ x,
-                                const double* __restrict__ q, float4* __restrict__ out) {
+__global__ void pack_dup_f32_kernel(int64_t n, int64_t n_pad, const double* __restrict__ x,
+                                    const double* __restrict__ q, ChargeDup* __restrict__ out) {
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n_pad;
-       i += (int64_t)gridDim.x * blockDim.x)
-    out[i] = i < n ? make_float4(static_cast<float>(x[3 * i]), static_cast<float>(x[3 * i + 1]),
-                                 static_cast<float>(x[3 * i + 2]), static_cast<float>(q[i]))
-                   : make_float4(1.0e4f, 1.0e4f, 1.0e4f, 0.f);
+       i += (int64_t)gridDim.x * blockDim.x) {
+    float v[4] = {1.0e4f, 1.0e4f, 1.0e4f, 0.f};  // zero charge far outside any box
+    if (i < n) {
+      v[0] = static_cast<float>(x[3 * i]);
+      v[1] = static_cast<float>(x[3 * i + 1]);
+      v[2] = static_cast<float>(x[3 * i + 2]);
+      v[3] = static_cast<float>(q[i]);
+    }
+    ChargeDup c;
+    c.xy = make_ulonglong2(dup2(v[0]), dup2(v[1]));
+    c.zq = make_ulonglong2(dup2(v[2]), dup2(v[3]));
+    out[i] = c;
+  }
 }
 
 __global__ void pack_f64_kernel(int64_t n, int64_t n_pad, const double* __restrict__ x,
@@ -240,7 +333,7 @@ cudaError_t launch_pack_charges(int prec, int64_t n, int64_t n_pad, const double
   if (n_pad <= 0) return cudaSuccess;
   const int blocks = static_cast<int>(std::min<int64_t>((n_pad + 255) / 256, 4096));
   if (prec == kFP32C)
-    pack_f32_kernel<<<blocks, 256, 0, s>>>(n, n_pad, x, q, static_cast<float4*>(packed));
+    pack_dup_f32_kernel<<<blocks, 256, 0, s>>>(n, n_pad, x, q, static_cast<ChargeDup*>(packed));
   else
     pack_f64_kernel<<<blocks, 256, 0, s>>>(n, n_pad, x, q, static_cast<Charge64*>(packed));
   return cudaGetLastError();

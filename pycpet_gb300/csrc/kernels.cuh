@@ -55,7 +55,8 @@ constexpr int kGridPPT = 4;  // points per thread
 constexpr int kGridTilePts = kGridThreads * kGridPPT;
 
 // grid.cu
-// Packs x[n][3], q[n] into float4 / Charge64 and fills [n, n_pad) with zero
+// Packs x[n][3], q[n] for the grid kernels (32-byte records: Charge64, or the
+// FP32C record with every component duplicated) and fills [n, n_pad) with zero
 // charges placed far outside any box (they contribute exactly zero).
 cudaError_t launch_pack_charges(int prec, int64_t n, int64_t n_pad, const double* x,
                                 const double* q, void* packed, cudaStream_t s);
@@ -66,6 +67,19 @@ cudaError_t launch_grid_final(int kind, int n_final, const GridFinal* fin,
                               const double* partial, double* out, cudaStream_t s);
 
 // topo.cu
+// One frame of a streamline launch (device table for multi-frame launches).
+struct TopoFrame {
+  int64_t packed_off;  // first packed element (FP32C: float4 index of the pair block; FP64: Charge64)
+  int64_t line_off;    // first line of the frame in starts / n_iter / result
+  int32_t n_pad;       // padded charge count (a multiple of topo_charge_pad(prec))
+  int32_t n_lines;
+  int32_t resident;    // 1: the frame's charges are staged in shared memory
+  int32_t pad_;
+  double step;
+  double half[3];
+};
+static_assert(sizeof(TopoFrame) == 64, "TopoFrame layout");
+
 struct TopoParams {
   int n_lines;
   int n_charges;
@@ -77,12 +91,26 @@ struct TopoParams {
   double* result;            // [L][2]  {distance, mean curvature}
   double* ends;              // [L][3] or null
   int32_t* steps;            // [L] or null (Euler steps of the main loop)
-  int* queue;                // work-queue counter (zeroed by the launcher)
+  int* queue;                // work-queue counter(s), one per frame (zeroed by the caller)
   int* status;
+  const TopoFrame* frames;   // device frame table (multi-frame launches) or null
+  int n_frames;              // frames in the table
+  int max_resident_pad;      // largest n_pad of a resident frame (shared-memory size)
 };
+// Single frame: p.frames == null, the frame is described by n_charges/step/half.
 cudaError_t launch_topo(int prec, const TopoParams& p, int num_sms, cudaStream_t s);
+// Multi-frame: p.frames/n_frames/queue[n_frames]/max_resident_pad set by the caller.
+cudaError_t launch_topo_frames(int prec, const TopoParams& p, int num_sms, cudaStream_t s);
+// Packs the charges of every frame of a table (host copy `frames`, device copy `d_frames`,
+// source offsets src_off[f] into x/q) into the streamline layout.
+cudaError_t launch_pack_topo_frames(int prec, int n_frames, const TopoFrame* d_frames,
+                                    const int64_t* d_src, const double* x, const double* q,
+                                    void* packed, int max_pairs, cudaStream_t s);
 size_t topo_resident_limit(int prec);  // max charges held resident in shared memory
-int topo_charge_pad();                 // packed charge arrays are padded to this multiple
+int topo_charge_pad(int prec);         // packed charge arrays are padded to this multiple
+// Packs charges in the streamline kernel's layout (FP32C: pair layout; FP64: Charge64).
+cudaError_t launch_pack_topo(int prec, int64_t n, int64_t n_pad, const double* x, const double* q,
+                             void* packed, cudaStream_t s);
 
 // api.cu: records `msg` as the calling thread's last error and returns `code`.
 int set_error(int code, const char* msg);

@@ -92,11 +92,11 @@ extern "C" int cpetgb_topo_lines_noalloc(int precision, int n_lines, int n_charg
   }
   cudaStream_t s = static_cast<cudaStream_t>(stream);
   int* counters = reinterpret_cast<int*>(base + kNoAllocChargeBytes);  // [0] queue, [1] status
-  const int pad = topo_charge_pad();
+  const int pad = topo_charge_pad(precision);
   const int64_t n_pad = ((std::max(n_charges, 1) + int64_t(pad) - 1) / pad) * pad;
 
   cudaError_t e = cudaMemsetAsync(counters, 0, 2 * sizeof(int), s);
-  if (e == cudaSuccess) e = launch_pack_charges(precision, n_charges, n_pad, x, q, base, s);
+  if (e == cudaSuccess) e = launch_pack_topo(precision, n_charges, n_pad, x, q, base, s);
   if (e == cudaSuccess) {
     TopoParams p;
     p.n_lines = n_lines;

@@ -45,9 +45,10 @@ namespace {
 
 constexpr int kTopoThreads = 512;
 constexpr int kTopoWarps = kTopoThreads / 32;
-constexpr int kLaneTile = 8;                   // charges per lane between Kahan steps
-constexpr int kChargePad = 32 * kLaneTile;     // resident charge array padding
-constexpr int kSlots = 4;                      // line slots per warp
+constexpr int kLanePairs = 16;                  // charge pairs per lane between Kahan steps
+constexpr int kChargePad32 = 32 * kLanePairs * 2;  // FP32C frames: multiple of 1024 charges
+constexpr int kChargePad64 = 256;               // FP64 frames
+constexpr int kSlots = 4;                       // line slots per warp
 
 enum Phase : int { kMain = 0, kStart1 = 1, kStart2 = 2, kEnd1 = 3, kEnd2 = 4 };
 
@@ -60,6 +61,20 @@ __device__ __forceinline__ bool outside(const double p[3], const double h[3]) {
          p[2] > h[2];
 }
 
+// Exact strict box test from the FP32 image pf = RN(p) of an FP64 position:
+// RN is monotonic, so |pf| > RN(h) implies |p| > h and |pf| < RN(h) implies
+// |p| < h; only a tie needs the FP64 comparison.
+__device__ __forceinline__ bool outside_fast(const double p[3], const float pf[3],
+                                             const double h[3], const float hf[3]) {
+  bool out = false;
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    const float a = fabsf(pf[k]);
+    if (a > hf[k] || (a == hf[k] && fabs(p[k]) > h[k])) out = true;
+  }
+  return out;
+}
+
 __device__ __forceinline__ double curve_f64(const double a[3], const double b[3]) {
   const double c0 = a[1] * b[2] - a[2] * b[1];
   const double c1 = a[2] * b[0] - a[0] * b[2];
@@ -69,6 +84,15 @@ __device__ __forceinline__ double curve_f64(const double a[3], const double b[3]
   return nc / (na * na * na);
 }
 
+// The frame a CTA is working on (uniform across the CTA).
+struct FrameCtx {
+  int64_t line_off;
+  int n_lines;
+  double step;
+  double half[3];
+  float hf[3];  // RN(half): the FP32 side of the exact box test
+};
+
 // Per-lane slot state (meaningful in lanes 0..S-1 only).
 struct Slot {
   int line;     // -1 = idle
@@ -76,16 +100,24 @@ struct Slot {
   int steps;
   int cap;
   double pos[3];  // where the next field evaluation happens
+  float posf[3];  // its FP32 image (FP32C pair terms)
 };
+
+__device__ __forceinline__ void set_pos(Slot& sl, const double v[3]) {
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    sl.pos[k] = v[k];
+    sl.posf[k] = static_cast<float>(v[k]);
+  }
+}
 
 __device__ void slot_load(Slot& sl, SlotRec& rec, int line, const TopoParams& p) {
   sl.line = line;
   if (line < 0) return;
   const double* s = p.starts + 3 * static_cast<int64_t>(line);
-  for (int k = 0; k < 3; ++k) {
-    rec.x0[k] = s[k];
-    sl.pos[k] = s[k];
-  }
+  double st[3];
+  for (int k = 0; k < 3; ++k) rec.x0[k] = st[k] = s[k];
+  set_pos(sl, st);
   sl.cap = max(p.n_iter[line], 0);
   if (sl.cap > kMaxLineCap) {  // refuse rather than run for hours
     atomicCAS(p.status, kDevOk, kDevBadCap);
@@ -102,7 +134,9 @@ __device__ void slot_load(Slot& sl, SlotRec& rec, int line, const TopoParams& p)
 
 // Advance one slot given the new position `nx` (= pos + step vector).
 // Returns true when the line has finished (result written).
-__device__ bool slot_advance(Slot& sl, SlotRec& rec, const double nx[3], const TopoParams& p) {
+template <bool FAST_BOX>
+__device__ bool slot_advance(Slot& sl, SlotRec& rec, const double nx[3], const TopoParams& p,
+                             const FrameCtx& fc) {
   switch (sl.phase) {
     case kMain: {
       sl.steps += 1;
@@ -110,33 +144,32 @@ __device__ bool slot_advance(Slot& sl, SlotRec& rec, const double nx[3], const T
         for (int k = 0; k < 3; ++k) rec.xip[k] = nx[k];
       if (sl.steps == 2)
         for (int k = 0; k < 3; ++k) rec.xipp[k] = nx[k];
-      if (outside(nx, p.half) || sl.steps >= sl.cap) {
+      set_pos(sl, nx);
+      const bool out =
+          FAST_BOX ? outside_fast(sl.pos, sl.posf, fc.half, fc.hf) : outside(nx, fc.half);
+      if (out || sl.steps >= sl.cap) {
         for (int k = 0; k < 3; ++k) rec.xend[k] = nx[k];
         if (sl.steps >= 2) {
-          sl.phase = kEnd1;
-          for (int k = 0; k < 3; ++k) sl.pos[k] = rec.xend[k];
+          sl.phase = kEnd1;  // next evaluation at the end point (= nx)
         } else {
-          sl.phase = kStart2;
-          for (int k = 0; k < 3; ++k) sl.pos[k] = rec.xip[k];
+          sl.phase = kStart2;  // steps == 1: the end point is also x_init_plus
         }
-      } else {
-        for (int k = 0; k < 3; ++k) sl.pos[k] = nx[k];
       }
       return false;
     }
     case kStart1:
-      for (int k = 0; k < 3; ++k) rec.xip[k] = sl.pos[k] = nx[k];
+      for (int k = 0; k < 3; ++k) rec.xip[k] = nx[k];
+      set_pos(sl, nx);
       sl.phase = kStart2;
       return false;
     case kStart2:
-      for (int k = 0; k < 3; ++k) {
-        rec.xipp[k] = nx[k];
-        sl.pos[k] = rec.xend[k];
-      }
+      for (int k = 0; k < 3; ++k) rec.xipp[k] = nx[k];
+      set_pos(sl, rec.xend);
       sl.phase = kEnd1;
       return false;
     case kEnd1:
-      for (int k = 0; k < 3; ++k) rec.xe1[k] = sl.pos[k] = nx[k];
+      for (int k = 0; k < 3; ++k) rec.xe1[k] = nx[k];
+      set_pos(sl, nx);
       sl.phase = kEnd2;
       return false;
     default: {  // kEnd2: nx is the second step after the end point
@@ -164,61 +197,88 @@ __device__ bool slot_advance(Slot& sl, SlotRec& rec, const double nx[3], const T
 // Field sweep over the charges for NA active slots.
 // ---------------------------------------------------------------------------
 
-// FP32C, charges resident in shared memory (padded to kChargePad).
+// FP32C.  Charges in "pair" layout: A[p] = {x_2p, x_2p+1, y_2p, y_2p+1},
+// B[p] = {z_2p, z_2p+1, q_2p, q_2p+1}, so each 64-bit half of a 16-byte load is
+// a ready operand of the packed f32x2 instructions: one instruction evaluates
+// a pair term for two charges.  Lanes take pairs lane-strided; every
+// kLanePairs pairs the two packed streams are added and Kahan-accumulated.
 template <int NA>
-__device__ __forceinline__ void sweep_f32(const float4* __restrict__ sm, int n_pad, int lane,
-                                          const float (&ex)[kSlots][3], float (&hi)[kSlots][3],
-                                          float (&lo)[kSlots][3]) {
+__device__ __forceinline__ void sweep_f32x2(const ulonglong2* __restrict__ A,
+                                            const ulonglong2* __restrict__ B, int n_pairs,
+                                            int lane, const uint64_t (&ex2)[kSlots][3],
+                                            float& total) {
   float acc[NA][3], cmp[NA][3];
 #pragma unroll
   for (int e = 0; e < NA; ++e)
 #pragma unroll
     for (int c = 0; c < 3; ++c) acc[e][c] = cmp[e][c] = 0.f;
 
-  for (int base = lane; base < n_pad; base += 32 * kLaneTile) {
-    float part[NA][3];
+  for (int base = lane; base < n_pairs; base += 32 * kLanePairs) {
+    uint64_t part[NA][3];
 #pragma unroll
     for (int e = 0; e < NA; ++e)
 #pragma unroll
-      for (int c = 0; c < 3; ++c) part[e][c] = 0.f;
-#pragma unroll
-    for (int i = 0; i < kLaneTile; ++i) {
-      const float4 ch = sm[base + 32 * i];
+      for (int c = 0; c < 3; ++c) part[e][c] = 0ull;
+#pragma unroll 4
+    for (int i = 0; i < kLanePairs; ++i) {
+      const ulonglong2 a = A[base + 32 * i];  // {x pair, y pair}
+      const ulonglong2 b = B[base + 32 * i];  // {z pair, q pair}
 #pragma unroll
       for (int e = 0; e < NA; ++e) {
-        // explicit roundings: a line's result does not depend on which
-        // other slots share its warp
-        const float dx = __fsub_rn(ex[e][0], ch.x);
-        const float dy = __fsub_rn(ex[e][1], ch.y);
-        const float dz = __fsub_rn(ex[e][2], ch.z);
-        const float r2 = __fmaf_rn(dx, dx, __fmaf_rn(dy, dy, __fmul_rn(dz, dz)));
-        const float ri = rsqrt_mufu(r2);
-        const float w = __fmul_rn(__fmul_rn(ch.w, ri), __fmul_rn(ri, ri));
-        part[e][0] = __fmaf_rn(w, dx, part[e][0]);
-        part[e][1] = __fmaf_rn(w, dy, part[e][1]);
-        part[e][2] = __fmaf_rn(w, dz, part[e][2]);
+        const uint64_t dx = sub2(ex2[e][0], a.x);
+        const uint64_t dy = sub2(ex2[e][1], a.y);
+        const uint64_t dz = sub2(ex2[e][2], b.x);
+        const uint64_t r2 = fma2(dx, dx, fma2(dy, dy, mul2(dz, dz)));
+        const uint64_t ri = rsqrt2(r2);
+        const uint64_t w = mul2(mul2(b.y, ri), mul2(ri, ri));
+        part[e][0] = fma2(w, dx, part[e][0]);
+        part[e][1] = fma2(w, dy, part[e][1]);
+        part[e][2] = fma2(w, dz, part[e][2]);
       }
     }
 #pragma unroll
     for (int e = 0; e < NA; ++e)
 #pragma unroll
-      for (int c = 0; c < 3; ++c) kahan_add(acc[e][c], cmp[e][c], part[e][c]);
-  }
-  // Lane partial = acc - cmp as an unevaluated pair; error-free butterfly.
-#pragma unroll
-  for (int e = 0; e < NA; ++e)
-#pragma unroll
-    for (int c = 0; c < 3; ++c) {
-      float h = acc[e][c], l = -cmp[e][c];
-#pragma unroll
-      for (int off = 16; off >= 1; off >>= 1) {
-        const float oh = __shfl_xor_sync(0xffffffffu, h, off);
-        const float ol = __shfl_xor_sync(0xffffffffu, l, off);
-        pair_add(h, l, oh, ol);
+      for (int c = 0; c < 3; ++c) {
+        float lo, hi2;
+        upk2(part[e][c], lo, hi2);
+        kahan_add(acc[e][c], cmp[e][c], __fadd_rn(lo, hi2));
       }
-      hi[e][c] = h;
-      lo[e][c] = l;
+  }
+  // Lane partials (acc - cmp, unevaluated pairs) as 16 values v = 3e + c,
+  // reduced across the warp by a reduce-scatter of error-free pair additions:
+  // each level halves the values a lane keeps; afterwards lanes 2v and 2v+1
+  // hold the total of value v.
+  float h[16], l[16];
+#pragma unroll
+  for (int v = 0; v < 16; ++v) {
+    const int e = v / 3, c = v % 3;
+    h[v] = (e < NA) ? acc[e < NA ? e : 0][c] : 0.f;
+    l[v] = (e < NA) ? -cmp[e < NA ? e : 0][c] : 0.f;
+  }
+#pragma unroll
+  for (int lvl = 0, half = 8; lvl < 4; ++lvl, half >>= 1) {
+    const int off = 16 >> lvl;
+    const bool upper = (lane & off) != 0;
+#pragma unroll
+    for (int j = 0; j < half; ++j) {
+      const float sh = upper ? h[j] : h[j + half];
+      const float sl = upper ? l[j] : l[j + half];
+      const float kh = upper ? h[j + half] : h[j];
+      const float kl = upper ? l[j + half] : l[j];
+      const float rh = __shfl_xor_sync(0xffffffffu, sh, off);
+      const float rl = __shfl_xor_sync(0xffffffffu, sl, off);
+      h[j] = kh;
+      l[j] = kl;
+      pair_add(h[j], l[j], rh, rl);
     }
+  }
+  {
+    const float rh = __shfl_xor_sync(0xffffffffu, h[0], 1);
+    const float rl = __shfl_xor_sync(0xffffffffu, l[0], 1);
+    pair_add(h[0], l[0], rh, rl);
+  }
+  total = h[0];
 }
 
 // FP64: charges from global memory (padded with zero charges far away).
@@ -260,172 +320,337 @@ __device__ __forceinline__ void sweep_f64(const Charge64* __restrict__ g, int n_
 // ---------------------------------------------------------------------------
 // Persistent kernel.
 // ---------------------------------------------------------------------------
-template <int PREC, bool RESIDENT>
-__global__ void __launch_bounds__(kTopoThreads, 1) topo_kernel(TopoParams p, int n_pad) {
-  extern __shared__ __align__(128) unsigned char smem_raw[];
-  const int lane = threadIdx.x & 31;
-  const int warp = threadIdx.x >> 5;
-  SlotRec* recs = reinterpret_cast<SlotRec*>(smem_raw);  // [kTopoWarps][kSlots]
-  const size_t rec_bytes = sizeof(SlotRec) * kTopoWarps * kSlots;
-  uint64_t* bar = reinterpret_cast<uint64_t*>(smem_raw + rec_bytes);
-  float4* sm_ch = reinterpret_cast<float4*>(smem_raw + rec_bytes + 128);
-  const float4* ch32 = RESIDENT ? sm_ch : static_cast<const float4*>(p.packed);
 
-  if constexpr (PREC == kFP32C && RESIDENT) {
-    // Resident charges: bulk async copy of the packed frame, pad by stores.
-    const int n = p.n_charges;
-    if (threadIdx.x == 0) {
-      mbar_init(bar, 1);
-      fence_mbar_init();
-    }
-    __syncthreads();
-    if (threadIdx.x == 0) {
-      const uint32_t total = static_cast<uint32_t>(n) * 16u;
-      mbar_arrive_expect_tx(bar, total);
-      const char* src = static_cast<const char*>(p.packed);
-      constexpr uint32_t kChunk = 32768;
-      for (uint32_t off = 0; off < total; off += kChunk)
-        bulk_g2s(reinterpret_cast<char*>(sm_ch) + off, src + off, min(kChunk, total - off), bar);
-    }
-    for (int j = n + threadIdx.x; j < n_pad; j += blockDim.x)
-      sm_ch[j] = make_float4(1.0e4f, 1.0e4f, 1.0e4f, 0.f);
-    const bool mine = mbar_wait(bar, 0, p.status);
-    if (!__syncthreads_and(mine)) return;
-  }
-
-  SlotRec* my_rec = recs + warp * kSlots + (lane < kSlots ? lane : 0);
+// One line slot set per warp; processes the lines of frame `fc` (charge
+// arrays chA/chB in the FP32C pair layout, or g in Charge64) until the frame's
+// queue is exhausted and the warp's slots are drained.
+template <int PREC>
+__device__ __forceinline__ void run_frame(const TopoParams& p, const FrameCtx& fc, int* queue,
+                                          const ulonglong2* chA, const ulonglong2* chB,
+                                          const ulonglong2* smA, const ulonglong2* smB,
+                                          bool resident, int n_pad, SlotRec* my_rec, int lane) {
   Slot sl;
   sl.line = -1;
   sl.phase = kMain;
   sl.steps = sl.cap = 0;
   sl.pos[0] = sl.pos[1] = sl.pos[2] = 0.0;
+  sl.posf[0] = sl.posf[1] = sl.posf[2] = 0.f;
   if (lane < kSlots) {
-    const int li = atomicAdd(p.queue, 1);
-    slot_load(sl, *my_rec, li < p.n_lines ? li : -1, p);
+    const int li = atomicAdd(queue, 1);
+    slot_load(sl, *my_rec, li < fc.n_lines ? static_cast<int>(fc.line_off + li) : -1, p);
   }
-
   for (;;) {
     const unsigned active = __ballot_sync(0xffffffffu, lane < kSlots && sl.line >= 0);
     const int na = __popc(active);
     if (na == 0) break;
-    // Evaluation positions of the active slots, broadcast to all lanes.
-    using Real = typename std::conditional<PREC == kFP32C, float, double>::type;
-    Real ex[kSlots][3];
+    // owner lane of each active slot, in order; this lane's rank among them
+    int src_of[kSlots];
     int my_rank = -1;
     {
       unsigned m = active;
 #pragma unroll
       for (int e = 0; e < kSlots; ++e) {
-        const int src = m ? (__ffs(m) - 1) : 0;
+        src_of[e] = m ? (__ffs(m) - 1) : 0;
         if (m) m &= m - 1;
-#pragma unroll
-        for (int c = 0; c < 3; ++c)
-          ex[e][c] = static_cast<Real>(__shfl_sync(0xffffffffu, sl.pos[c], src));
-        if (src == lane && e < na) my_rank = e;
+        if (src_of[e] == lane && e < na) my_rank = e;
       }
     }
 
-    double E[3] = {0.0, 0.0, 0.0};
-    float Ef[3] = {0.f, 0.f, 0.f};
+    double nx[3];
     if constexpr (PREC == kFP32C) {
-      float hi[kSlots][3], lo[kSlots][3];
-      switch (na) {
-        case 1: sweep_f32<1>(ch32, n_pad, lane, ex, hi, lo); break;
-        case 2: sweep_f32<2>(ch32, n_pad, lane, ex, hi, lo); break;
-        case 3: sweep_f32<3>(ch32, n_pad, lane, ex, hi, lo); break;
-        default: sweep_f32<4>(ch32, n_pad, lane, ex, hi, lo); break;
-      }
+      uint64_t ex2[kSlots][3];
 #pragma unroll
       for (int e = 0; e < kSlots; ++e)
-        if (e == my_rank)
 #pragma unroll
-          for (int c = 0; c < 3; ++c) Ef[c] = hi[e][c];
+        for (int c = 0; c < 3; ++c) {
+          const float v = __shfl_sync(0xffffffffu, sl.posf[c], src_of[e]);
+          ex2[e][c] = pk2(v, v);
+        }
+      float total;
+      const int n_pairs = n_pad / 2;
+      if (resident) {
+        switch (na) {
+          case 1: sweep_f32x2<1>(smA, smB, n_pairs, lane, ex2, total); break;
+          case 2: sweep_f32x2<2>(smA, smB, n_pairs, lane, ex2, total); break;
+          case 3: sweep_f32x2<3>(smA, smB, n_pairs, lane, ex2, total); break;
+          default: sweep_f32x2<4>(smA, smB, n_pairs, lane, ex2, total); break;
+        }
+      } else {
+        switch (na) {
+          case 1: sweep_f32x2<1>(chA, chB, n_pairs, lane, ex2, total); break;
+          case 2: sweep_f32x2<2>(chA, chB, n_pairs, lane, ex2, total); break;
+          case 3: sweep_f32x2<3>(chA, chB, n_pairs, lane, ex2, total); break;
+          default: sweep_f32x2<4>(chA, chB, n_pairs, lane, ex2, total); break;
+        }
+      }
+      // component c of slot rank e sits in lanes 2(3e + c), 2(3e + c) + 1
+      float Ef[3];
+      const int rk = my_rank >= 0 ? my_rank : 0;
+#pragma unroll
+      for (int c = 0; c < 3; ++c) Ef[c] = __shfl_sync(0xffffffffu, total, 2 * (3 * rk + c));
+      if (my_rank >= 0) {
+        // step vector in FP32 (the factor k does not change the direction)
+        const float n2 = __fmaf_rn(Ef[0], Ef[0], __fmaf_rn(Ef[1], Ef[1], __fmul_rn(Ef[2], Ef[2])));
+        const float s = __fdiv_rn(static_cast<float>(fc.step), __fsqrt_rn(n2));
+#pragma unroll
+        for (int c = 0; c < 3; ++c) nx[c] = sl.pos[c] + static_cast<double>(__fmul_rn(Ef[c], s));
+      }
     } else {
+      double ex[kSlots][3];
+#pragma unroll
+      for (int e = 0; e < kSlots; ++e)
+#pragma unroll
+        for (int c = 0; c < 3; ++c) ex[e][c] = __shfl_sync(0xffffffffu, sl.pos[c], src_of[e]);
       double Es[kSlots][3];
-      const Charge64* g = static_cast<const Charge64*>(p.packed);
+      const Charge64* g = reinterpret_cast<const Charge64*>(chA);
       switch (na) {
         case 1: sweep_f64<1>(g, n_pad, lane, ex, Es); break;
         case 2: sweep_f64<2>(g, n_pad, lane, ex, Es); break;
         case 3: sweep_f64<3>(g, n_pad, lane, ex, Es); break;
         default: sweep_f64<4>(g, n_pad, lane, ex, Es); break;
       }
+      if (my_rank >= 0) {
+        double E[3] = {0.0, 0.0, 0.0};
 #pragma unroll
-      for (int e = 0; e < kSlots; ++e)
-        if (e == my_rank)
+        for (int e = 0; e < kSlots; ++e)
+          if (e == my_rank)
 #pragma unroll
-          for (int c = 0; c < 3; ++c) E[c] = Es[e][c];
+            for (int c = 0; c < 3; ++c) E[c] = Es[e][c];
+        const double n = sqrt(E[0] * E[0] + E[1] * E[1] + E[2] * E[2]);
+#pragma unroll
+        for (int c = 0; c < 3; ++c) nx[c] = sl.pos[c] + fc.step * E[c] / n;
+      }
     }
 
     if (my_rank >= 0) {
-      double nx[3];
-      if constexpr (PREC == kFP32C) {
-        // step vector in FP32 (E scaled by k does not change the direction)
-        const float n2 = Ef[0] * Ef[0] + Ef[1] * Ef[1] + Ef[2] * Ef[2];
-        const float s = __fdiv_rn(static_cast<float>(p.step), __fsqrt_rn(n2));
-#pragma unroll
-        for (int c = 0; c < 3; ++c) nx[c] = sl.pos[c] + static_cast<double>(Ef[c] * s);
-      } else {
-        const double n = sqrt(E[0] * E[0] + E[1] * E[1] + E[2] * E[2]);
-#pragma unroll
-        for (int c = 0; c < 3; ++c) nx[c] = sl.pos[c] + p.step * E[c] / n;
-      }
-      if (slot_advance(sl, *my_rec, nx, p)) {
-        const int li = atomicAdd(p.queue, 1);
-        slot_load(sl, *my_rec, li < p.n_lines ? li : -1, p);
+      if (slot_advance<PREC == kFP32C>(sl, *my_rec, nx, p, fc)) {
+        const int li = atomicAdd(queue, 1);
+        slot_load(sl, *my_rec, li < fc.n_lines ? static_cast<int>(fc.line_off + li) : -1, p);
       }
     }
     __syncwarp();
   }
 }
 
-size_t topo_smem_bytes(bool resident, int n_pad) {
-  size_t b = sizeof(SlotRec) * kTopoWarps * kSlots + 128;
-  if (resident) b += static_cast<size_t>(n_pad) * 16;
-  return b;
+// Frames are visited in table order; a CTA stays on a frame while its line
+// queue lasts, then moves on (after its own warps are done, so the shared
+// copy of the charges can be replaced).  Frames thus overlap only at their
+// tails and every frame switch costs a CTA one line's latency at most.
+template <int PREC, bool CAN_RESIDE>
+__global__ void __launch_bounds__(kTopoThreads, 1) topo_kernel(TopoParams p, TopoFrame frame0) {
+  extern __shared__ __align__(128) unsigned char smem_raw[];
+  __shared__ int s_skip;
+  const int lane = threadIdx.x & 31;
+  const int warp = threadIdx.x >> 5;
+  SlotRec* recs = reinterpret_cast<SlotRec*>(smem_raw);  // [kTopoWarps][kSlots]
+  const size_t rec_bytes = sizeof(SlotRec) * kTopoWarps * kSlots;
+  uint64_t* bar = reinterpret_cast<uint64_t*>(smem_raw + rec_bytes);
+  ulonglong2* sm_ch = reinterpret_cast<ulonglong2*>(smem_raw + rec_bytes + 128);
+  SlotRec* my_rec = recs + warp * kSlots + (lane < kSlots ? lane : 0);
+  const int n_frames = p.frames ? p.n_frames : 1;
+  uint32_t load_parity = 0;
+  if (CAN_RESIDE && threadIdx.x == 0) {
+    mbar_init(bar, 1);
+    fence_mbar_init();
+  }
+
+  for (int f = 0; f < n_frames; ++f) {
+    const TopoFrame fr = p.frames ? p.frames[f] : frame0;
+    int* queue = p.queue + f;
+    __syncthreads();  // the CTA's warps are done with the previous frame
+    if (threadIdx.x == 0) s_skip = (*reinterpret_cast<volatile int*>(queue) >= fr.n_lines) ? 1 : 0;
+    __syncthreads();
+    if (s_skip) continue;
+    const bool resident = CAN_RESIDE && fr.resident;
+    if (resident) {
+      if (threadIdx.x == 0) {
+        const uint32_t total = static_cast<uint32_t>(fr.n_pad) * 16u;
+        mbar_arrive_expect_tx(bar, total);
+        const char* src = static_cast<const char*>(p.packed) + fr.packed_off * 16;
+        constexpr uint32_t kChunk = 32768;
+        for (uint32_t off = 0; off < total; off += kChunk)
+          bulk_g2s(reinterpret_cast<char*>(sm_ch) + off, src + off, min(kChunk, total - off), bar);
+      }
+      const bool mine = mbar_wait(bar, load_parity, p.status);
+      load_parity ^= 1u;
+      if (!__syncthreads_and(mine)) return;
+    }
+    FrameCtx fc;
+    fc.line_off = fr.line_off;
+    fc.n_lines = fr.n_lines;
+    fc.step = fr.step;
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+      fc.half[k] = fr.half[k];
+      fc.hf[k] = static_cast<float>(fr.half[k]);
+    }
+    const size_t elem = (PREC == kFP32C) ? 16 : 32;
+    const ulonglong2* gA = reinterpret_cast<const ulonglong2*>(
+        static_cast<const char*>(p.packed) + fr.packed_off * elem);
+    const ulonglong2* gB = gA + fr.n_pad / 2;
+    run_frame<PREC>(p, fc, queue, gA, gB, sm_ch, sm_ch + fr.n_pad / 2, resident, fr.n_pad, my_rec,
+                    lane);
+  }
 }
 
-template <int PREC, bool RESIDENT>
-cudaError_t launch_topo_t(const TopoParams& p, int n_pad, int num_sms, cudaStream_t s) {
-  const size_t smem = topo_smem_bytes(RESIDENT, n_pad);
-  cudaError_t err = cudaFuncSetAttribute(topo_kernel<PREC, RESIDENT>,
+__global__ void pack_pairs_kernel(int64_t n, int64_t n_pad, const double* __restrict__ x,
+                                  const double* __restrict__ q, float4* __restrict__ out) {
+  const int64_t n_pairs = n_pad / 2;
+  for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < n_pairs;
+       p += (int64_t)gridDim.x * blockDim.x) {
+    float c[2][4];
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+      const int64_t i = 2 * p + h;
+      if (i < n) {
+        c[h][0] = static_cast<float>(x[3 * i]);
+        c[h][1] = static_cast<float>(x[3 * i + 1]);
+        c[h][2] = static_cast<float>(x[3 * i + 2]);
+        c[h][3] = static_cast<float>(q[i]);
+      } else {  // zero charge far outside any box
+        c[h][0] = c[h][1] = c[h][2] = 1.0e4f;
+        c[h][3] = 0.f;
+      }
+    }
+    out[p] = make_float4(c[0][0], c[1][0], c[0][1], c[1][1]);            // A
+    out[n_pairs + p] = make_float4(c[0][2], c[1][2], c[0][3], c[1][3]);  // B
+  }
+}
+
+size_t topo_smem_bytes(int max_resident_pad) {
+  return sizeof(SlotRec) * kTopoWarps * kSlots + 128 + static_cast<size_t>(max_resident_pad) * 16;
+}
+
+template <int PREC, bool CAN_RESIDE>
+cudaError_t launch_topo_t(const TopoParams& p, const TopoFrame& f0, int total_lines, int num_sms,
+                          cudaStream_t s) {
+  const size_t smem = topo_smem_bytes(CAN_RESIDE ? p.max_resident_pad : 0);
+  cudaError_t err = cudaFuncSetAttribute(topo_kernel<PREC, CAN_RESIDE>,
                                          cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          static_cast<int>(smem));
   if (err != cudaSuccess) return err;
   int per_sm = 1;
-  err = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, topo_kernel<PREC, RESIDENT>,
+  err = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, topo_kernel<PREC, CAN_RESIDE>,
                                                       kTopoThreads, smem);
   if (err != cudaSuccess) return err;
   per_sm = std::max(per_sm, 1);
-  const int max_useful = (p.n_lines + kTopoWarps * kSlots - 1) / (kTopoWarps * kSlots);
+  const int max_useful = (total_lines + kTopoWarps * kSlots - 1) / (kTopoWarps * kSlots);
   const int grid = std::max(1, std::min(num_sms * per_sm, max_useful));
-  topo_kernel<PREC, RESIDENT><<<grid, kTopoThreads, smem, s>>>(p, n_pad);
+  topo_kernel<PREC, CAN_RESIDE><<<grid, kTopoThreads, smem, s>>>(p, f0);
   return cudaGetLastError();
+}
+
+__global__ void pack_frames_kernel(int prec, const TopoFrame* __restrict__ frames,
+                                   const int64_t* __restrict__ src, const double* __restrict__ x,
+                                   const double* __restrict__ q, void* __restrict__ packed) {
+  const int f = blockIdx.y;
+  const TopoFrame fr = frames[f];
+  const int64_t off = src[2 * f], n = src[2 * f + 1];
+  const double* fx = x + 3 * off;
+  const double* fq = q + off;
+  if (prec == kFP32C) {
+    float4* out = static_cast<float4*>(packed) + fr.packed_off;
+    const int64_t n_pairs = fr.n_pad / 2;
+    for (int64_t pp = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; pp < n_pairs;
+         pp += (int64_t)gridDim.x * blockDim.x) {
+      float c[2][4];
+#pragma unroll
+      for (int h = 0; h < 2; ++h) {
+        const int64_t i = 2 * pp + h;
+        if (i < n) {
+          c[h][0] = static_cast<float>(fx[3 * i]);
+          c[h][1] = static_cast<float>(fx[3 * i + 1]);
+          c[h][2] = static_cast<float>(fx[3 * i + 2]);
+          c[h][3] = static_cast<float>(fq[i]);
+        } else {
+          c[h][0] = c[h][1] = c[h][2] = 1.0e4f;
+          c[h][3] = 0.f;
+        }
+      }
+      out[pp] = make_float4(c[0][0], c[1][0], c[0][1], c[1][1]);
+      out[n_pairs + pp] = make_float4(c[0][2], c[1][2], c[0][3], c[1][3]);
+    }
+  } else {
+    Charge64* out = static_cast<Charge64*>(packed) + fr.packed_off;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < fr.n_pad;
+         i += (int64_t)gridDim.x * blockDim.x) {
+      Charge64 c;
+      if (i < n) {
+        c.x = fx[3 * i];
+        c.y = fx[3 * i + 1];
+        c.z = fx[3 * i + 2];
+        c.q = fq[i];
+      } else {
+        c.x = c.y = c.z = 1.0e4;
+        c.q = 0.0;
+      }
+      out[i] = c;
+    }
+  }
 }
 
 }  // namespace
 
-int topo_charge_pad() { return kChargePad; }
+int topo_charge_pad(int prec) { return prec == kFP32C ? kChargePad32 : kChargePad64; }
 
 size_t topo_resident_limit(int prec) {
   if (prec != kFP32C) return 0;  // FP64 charges are read from global memory (L2)
   int dev = 0, optin = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
-  const size_t fixed = topo_smem_bytes(false, 0);
+  const size_t fixed = topo_smem_bytes(0) + 256;  // + static shared memory
   if (optin <= static_cast<int>(fixed)) return 0;
   size_t n = (static_cast<size_t>(optin) - fixed) / 16;
-  return (n / kChargePad) * kChargePad;
+  return (n / kChargePad32) * kChargePad32;
 }
 
-// p.packed must hold round_up(n_charges, kChargePad) packed charges, the tail
-// being zero charges placed far from the box (written by the pack kernel).
-cudaError_t launch_topo(int prec, const TopoParams& p, int num_sms, cudaStream_t s) {
-  if (p.n_lines <= 0) return cudaSuccess;
-  const int n_pad = ((p.n_charges + kChargePad - 1) / kChargePad) * kChargePad;
-  if (prec == kFP64) return launch_topo_t<kFP64, false>(p, n_pad, num_sms, s);
-  if (static_cast<size_t>(n_pad) <= topo_resident_limit(kFP32C))
-    return launch_topo_t<kFP32C, true>(p, n_pad, num_sms, s);
-  return launch_topo_t<kFP32C, false>(p, n_pad, num_sms, s);
+cudaError_t launch_pack_topo(int prec, int64_t n, int64_t n_pad, const double* x, const double* q,
+                             void* packed, cudaStream_t s) {
+  if (prec != kFP32C) return launch_pack_charges(prec, n, n_pad, x, q, packed, s);
+  if (n_pad <= 0) return cudaSuccess;
+  const int blocks = static_cast<int>(std::min<int64_t>((n_pad / 2 + 255) / 256, 4096));
+  pack_pairs_kernel<<<blocks, 256, 0, s>>>(n, n_pad, x, q, static_cast<float4*>(packed));
+  return cudaGetLastError();
+}
+
+cudaError_t launch_pack_topo_frames(int prec, int n_frames, const TopoFrame* d_frames,
+                                    const int64_t* d_src, const double* x, const double* q,
+                                    void* packed, int max_pairs, cudaStream_t s) {
+  if (n_frames <= 0) return cudaSuccess;
+  const int bx = std::max(1, std::min((max_pairs + 255) / 256, 256));
+  pack_frames_kernel<<<dim3(bx, n_frames), 256, 0, s>>>(prec, d_frames, d_src, x, q, packed);
+  return cudaGetLastError();
+}
+
+// Single frame: p.packed holds round_up(n_charges, topo_charge_pad(prec)) charges
+// packed by launch_pack_topo (the tail being zero charges far from the box).
+cudaError_t launch_topo(int prec, const TopoParams& p_in, int num_sms, cudaStream_t s) {
+  if (p_in.n_lines <= 0) return cudaSuccess;
+  TopoParams p = p_in;
+  const int pad = topo_charge_pad(prec);
+  TopoFrame f0;
+  f0.packed_off = 0;
+  f0.line_off = 0;
+  f0.n_pad = ((std::max(p.n_charges, 1) + pad - 1) / pad) * pad;
+  f0.n_lines = p.n_lines;
+  f0.resident = (prec == kFP32C && static_cast<size_t>(f0.n_pad) <= topo_resident_limit(kFP32C));
+  f0.pad_ = 0;
+  f0.step = p.step;
+  for (int k = 0; k < 3; ++k) f0.half[k] = p.half[k];
+  p.frames = nullptr;
+  p.n_frames = 1;
+  p.max_resident_pad = f0.resident ? f0.n_pad : 0;
+  if (prec == kFP64) return launch_topo_t<kFP64, false>(p, f0, p.n_lines, num_sms, s);
+  if (f0.resident) return launch_topo_t<kFP32C, true>(p, f0, p.n_lines, num_sms, s);
+  return launch_topo_t<kFP32C, false>(p, f0, p.n_lines, num_sms, s);
+}
+
+cudaError_t launch_topo_frames(int prec, const TopoParams& p, int num_sms, cudaStream_t s) {
+  if (p.n_frames <= 0 || p.n_lines <= 0) return cudaSuccess;
+  TopoFrame dummy{};
+  if (prec == kFP64) return launch_topo_t<kFP64, false>(p, dummy, p.n_lines, num_sms, s);
+  if (p.max_resident_pad > 0) return launch_topo_t<kFP32C, true>(p, dummy, p.n_lines, num_sms, s);
+  return launch_topo_t<kFP32C, false>(p, dummy, p.n_lines, num_sms, s);
 }
 
 }  // namespace cpetgb

@@ -116,3 +116,29 @@ def test_device_path(gpu_lib):
                      torch.from_numpy(q).cuda(), step, dims, precision="fp32c")
     synchronize()
     np.testing.assert_array_equal(dev.cpu().numpy(), host)
+
+
+def test_batch_of_frames_equals_single_frames(gpu_lib):
+    """Frames of different sizes (resident and streamed charges, uneven line
+    counts, different boxes and steps) in one launch give exactly the
+    per-frame results."""
+    from pycpet_gb300 import TopoBatch, topo_lines
+
+    specs = [(2000, 300, 1.5, 0.01), (15000, 60, 1.0, 0.02), (700, 1000, 0.5, 0.01), (9000, 1, 1.5, 0.01),
+             (3000, 0, 1.5, 0.01)]
+    frames = []
+    for i, (n, L, half, step) in enumerate(specs):
+        x, q, starts, caps, dims, _ = _case(n, max(L, 1), 100 + i, half=half, step=step)
+        frames.append({"x": x, "q": q, "starts": starts[:L], "n_iter": caps[:L], "step": step,
+                       "half_dims": dims})
+    for prec in ("fp32c", "fp64"):
+        tb = TopoBatch(frames, precision=prec)
+        res, steps = tb.run(return_steps=True)
+        for fr, r, s in zip(frames, tb.split(res), tb.split(steps)):
+            if len(fr["starts"]) == 0:
+                assert len(r) == 0
+                continue
+            single, ss = topo_lines(fr["starts"], fr["n_iter"], fr["x"], fr["q"], fr["step"], fr["half_dims"],
+                                    precision=prec, return_steps=True)
+            np.testing.assert_array_equal(s, ss)
+            np.testing.assert_array_equal(r, single)
