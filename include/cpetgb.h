@@ -124,6 +124,38 @@ int cpetgb_topo_batch(int precision, int mem, int n_frames, const int64_t* desc,
                       const double* params, const double* starts, const int32_t* n_iter,
                       const double* x, const double* q, double* result, double* ends,
                       int32_t* steps, void* stream);
+/* ---- autotuner table ------------------------------------------------------ */
+/* Tile shapes are chosen per (operation, precision, class, size bucket):
+ *   op 0 = grid sums: class = CPETGB_FIELD / CPETGB_ESP, size = pair evaluations
+ *          of the launch (buckets of x4 from 1e6); variants 0..5 = points per
+ *          thread {4, 8} x work items per SM {4, 8, 16} (default 1);
+ *   op 1 = streamlines: class = 1 if the frame's charges stay in shared memory,
+ *          size = lines (buckets of x4 from 1e3); variants 0..1 = line slots per
+ *          warp {4, 2} (default 0).
+ * pycpet_gb300.autotune times the candidates and fills the table. */
+int cpetgb_tune_key(int op, int precision, int cls, double size);
+int cpetgb_tune_variants(int op);
+int cpetgb_tune_set(int key, int variant);   /* variant -1 removes the entry */
+int cpetgb_tune_get(int key);                /* -1 when untuned */
+
+/* ---- prepared launches (CUDA graphs) ------------------------------------ */
+/* A plan binds DEVICE buffers once, builds the work decomposition and the
+ * scratch (cudaMalloc, held until cpetgb_plan_destroy), and captures the launch
+ * sequence (pack, kernel, reduction) into a CUDA graph.  cpetgb_plan_launch
+ * replays it on `stream`, reading the bound inputs as they are at that time
+ * (e.g. the next MD frame's coordinates written in place).  Arguments as
+ * cpetgb_grid_batch / cpetgb_topo_batch with mem = CPETGB_DEVICE. */
+typedef struct cpetgb_plan cpetgb_plan;
+int cpetgb_grid_plan_create(cpetgb_plan** plan, int kind, int precision, int clamp, int n_frames,
+                            const int64_t* desc, const double* points, const double* x,
+                            const double* q, double* out);
+int cpetgb_topo_plan_create(cpetgb_plan** plan, int precision, int n_frames, const int64_t* desc,
+                            const double* params, const double* starts, const int32_t* n_iter,
+                            const double* x, const double* q, double* result, double* ends,
+                            int32_t* steps);
+int cpetgb_plan_launch(cpetgb_plan* plan, void* stream);
+int cpetgb_plan_destroy(cpetgb_plan* plan);
+
 /* Streamlines for callers that must not have device memory allocated on their
  * behalf (device memory reserved up front by their own allocator, or a fixed
  * footprint after start-up).  No counterpart in the reference.  Same arguments

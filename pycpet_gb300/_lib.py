@@ -49,6 +49,14 @@ SIGNATURES = {
     "cpetgb_grid_batch": [_i, _i, _i, _i, _i, _vp, _vp, _vp, _vp, _vp, _vp],
     "cpetgb_topo_lines": [_i, _i, _i, _i, _vp, _vp, _d, _vp, _vp, _vp, _vp, _vp, _vp, _vp],
     "cpetgb_topo_batch": [_i, _i, _i, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp],
+    "cpetgb_tune_key": [_i, _i, _i, _d],
+    "cpetgb_tune_variants": [_i],
+    "cpetgb_tune_set": [_i, _i],
+    "cpetgb_tune_get": [_i],
+    "cpetgb_grid_plan_create": [_vp, _i, _i, _i, _i, _vp, _vp, _vp, _vp, _vp],
+    "cpetgb_topo_plan_create": [_vp, _i, _i, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp],
+    "cpetgb_plan_launch": [_vp, _vp],
+    "cpetgb_plan_destroy": [_vp],
     "cpetgb_topo_lines_noalloc": [_i, _i, _i, _vp, _vp, _d, _vp, _vp, _vp, _vp, _vp, _vp, _vp],
     "cpetgb_topo_hist2d": [_i, _i, _vp, _i, _i, _vp, _vp, _vp, _vp],
 }
@@ -74,7 +82,23 @@ def lib(path: str | None = None):
         fn.argtypes = argtypes
         fn.restype = ctypes.c_int
     _lib, _path = L, so
+    _load_tuned_table()
     return L
+
+
+def _load_tuned_table():
+    """Loads the autotuner table for this GPU (the user's cache, else the one
+    shipped for the model), when a CUDA device is visible."""
+    try:
+        import torch
+
+        if not torch.cuda.is_available():
+            return
+        from . import autotune
+
+        autotune.load_default()
+    except Exception:  # a missing or unreadable table only means default shapes
+        pass
 
 
 def last_error() -> str:

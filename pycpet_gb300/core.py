@@ -134,7 +134,7 @@ class GridBatch:
     into torch CUDA tensors and ``run()`` stays on the device.
     """
 
-    def __init__(self, frames, kind="field", precision="fp32c", clamp=True, device=False):
+    def __init__(self, frames, kind="field", precision="fp32c", clamp=True, device=False, graph=False):
         self.kind = FIELD if kind == "field" else ESP
         self.prec = precision_code(precision)
         self.clamp = int(bool(clamp))
@@ -163,12 +163,21 @@ class GridBatch:
             self.x = torch.from_numpy(self.x).cuda()
             self.q = torch.from_numpy(self.q).cuda()
             self.out = torch.empty((po, self.nc), dtype=torch.float64, device=self.points.device)
+        self.plan = None
+        if graph:
+            if not device:
+                raise ValueError("graph=True needs device=True (a plan binds device buffers)")
+            self.plan = _Plan.grid(self.kind, self.prec, self.clamp, self.desc, self.points, self.x, self.q,
+                                   self.out)
 
     @property
     def pair_evals(self) -> int:
         return int(np.sum(self.desc[:, 1] * self.desc[:, 3]))
 
     def run(self, out=None):
+        if self.plan is not None and out is None:
+            self.plan.launch(self.points)
+            return self.out
         if self.device:
             out = self.out if out is None else out
             with __import__("torch").cuda.device(self.points.device):
@@ -236,6 +245,50 @@ def topo_lines(starts, n_iter, x, q, step, half_dims, precision="fp32c", return_
     return out[0] if len(out) == 1 else tuple(out)
 
 
+class _Plan:
+    """A CUDA-graph plan of the library (cpetgb_plan) bound to device tensors."""
+
+    def __init__(self, handle, keep):
+        self.handle = handle
+        self._keep = keep  # tensors the graph reads / writes
+
+    @classmethod
+    def grid(cls, kind, prec, clamp, desc, points, x, q, out):
+        import ctypes
+
+        h = ctypes.c_void_p()
+        with __import__("torch").cuda.device(points.device):
+            check(lib().cpetgb_grid_plan_create(ctypes.byref(h), kind, prec, clamp, len(desc), desc.ctypes.data,
+                                                points.data_ptr(), x.data_ptr(), q.data_ptr(), out.data_ptr()))
+        return cls(h, (desc, points, x, q, out))
+
+    @classmethod
+    def topo(cls, prec, desc, params, starts, n_iter, x, q, result, steps):
+        import ctypes
+
+        h = ctypes.c_void_p()
+        with __import__("torch").cuda.device(starts.device):
+            check(lib().cpetgb_topo_plan_create(ctypes.byref(h), prec, len(desc), desc.ctypes.data,
+                                                params.ctypes.data, starts.data_ptr(), n_iter.data_ptr(),
+                                                x.data_ptr(), q.data_ptr(), result.data_ptr(), None,
+                                                steps.data_ptr() if steps is not None else None))
+        return cls(h, (desc, params, starts, n_iter, x, q, result, steps))
+
+    def launch(self, like):
+        import torch
+
+        with torch.cuda.device(like.device):
+            check(lib().cpetgb_plan_launch(self.handle, _stream_of(like)))
+
+    def __del__(self):
+        if getattr(self, "handle", None):
+            try:
+                lib().cpetgb_plan_destroy(self.handle)
+            except Exception:
+                pass
+            self.handle = None
+
+
 class TopoBatch:
     """Streamlines of many frames in one persistent launch (frame descriptor table).
 
@@ -245,7 +298,7 @@ class TopoBatch:
     With ``device=True`` the inputs live in torch CUDA tensors.
     """
 
-    def __init__(self, frames, precision="fp32c", device=False):
+    def __init__(self, frames, precision="fp32c", device=False, graph=False):
         self.prec = precision_code(precision)
         starts, caps, xs, qs, desc, params = [], [], [], [], [], []
         lo = co = 0
@@ -276,8 +329,21 @@ class TopoBatch:
             self.n_iter = torch.from_numpy(self.n_iter).cuda()
             self.x = torch.from_numpy(self.x).cuda()
             self.q = torch.from_numpy(self.q).cuda()
+        self.plan = None
+        if graph:
+            if not device:
+                raise ValueError("graph=True needs device=True (a plan binds device buffers)")
+            import torch
+
+            self.result = torch.empty((self.n_lines, 2), dtype=torch.float64, device=self.starts.device)
+            self.steps = torch.empty((self.n_lines,), dtype=torch.int32, device=self.starts.device)
+            self.plan = _Plan.topo(self.prec, self.desc, self.params, self.starts, self.n_iter, self.x, self.q,
+                                   self.result, self.steps)
 
     def run(self, return_steps=False):
+        if self.plan is not None:
+            self.plan.launch(self.starts)
+            return (self.result, self.steps) if return_steps else self.result
         if self.device:
             import torch
 

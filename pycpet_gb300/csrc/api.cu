@@ -13,6 +13,7 @@
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
+#include <map>
 #include <mutex>
 #include <string>
 #include <vector>
@@ -160,16 +161,46 @@ struct GridPlan {
   int n_slots = 0;
 };
 
-void plan_grid(int n_frames, const int64_t* desc, int sms, GridPlan& plan) {
+// ---------------------------------------------------------------------------
+// Autotuner table: (operation, precision, class, size bucket) -> variant.
+// Filled by pycpet_gb300.autotune (timed candidates), read at every launch.
+// ---------------------------------------------------------------------------
+std::mutex g_tune_mu;
+std::map<int, int> g_tune;
+
+constexpr int kOpGrid = 0, kOpTopo = 1;
+constexpr int kGridVariants = 6;  // points per thread {4, 8} x work items per SM {4, 8, 16}
+constexpr int kTopoVariants = 2;  // line slots per warp {4, 2}
+
+int size_bucket(double v, double base) {
+  if (!(v > base)) return 0;
+  const int b = static_cast<int>(std::floor(std::log(v / base) / std::log(4.0)));
+  return std::min(std::max(b, 0), 15);
+}
+
+int tune_key(int op, int prec, int cls, double size) {
+  const int b = op == kOpGrid ? size_bucket(size, 1e6) : size_bucket(size, 1e3);
+  return (op << 12) | (prec << 8) | ((cls & 15) << 4) | b;
+}
+
+int tune_lookup(int key) {
+  std::lock_guard<std::mutex> lock(g_tune_mu);
+  auto it = g_tune.find(key);
+  return it == g_tune.end() ? -1 : it->second;
+}
+
+void plan_grid(int n_frames, const int64_t* desc, int sms, GridPlan& plan, int ppt,
+               int items_per_sm) {
   double total = 0.0;
   for (int f = 0; f < n_frames; ++f) total += double(desc[4 * f + 1]) * double(desc[4 * f + 3]);
-  // Aim for about 8 items per SM so the largest-first order balances the tail.
-  const double target = std::max(1.0, total / (double(std::max(sms, 1)) * 8.0));
+  const int tile = kGridThreads * ppt;
+  // about items_per_sm items per SM so the largest-first order balances the tail
+  const double target = std::max(1.0, total / (double(std::max(sms, 1)) * items_per_sm));
   for (int f = 0; f < n_frames; ++f) {
     const int64_t co = desc[4 * f + 0], n = desc[4 * f + 1];
     const int64_t po = desc[4 * f + 2], P = desc[4 * f + 3];
-    for (int64_t pb = 0; pb < P; pb += kGridTilePts) {
-      const int pc = static_cast<int>(std::min<int64_t>(kGridTilePts, P - pb));
+    for (int64_t pb = 0; pb < P; pb += tile) {
+      const int pc = static_cast<int>(std::min<int64_t>(tile, P - pb));
       int64_t split = 1;
       if (n > 0) {
         const double cost = double(pc) * double(n);
@@ -203,6 +234,12 @@ void plan_grid(int n_frames, const int64_t* desc, int sms, GridPlan& plan) {
   });
 }
 
+double grid_pair_evals(int n_frames, const int64_t* desc) {
+  double total = 0.0;
+  for (int f = 0; f < n_frames; ++f) total += double(desc[4 * f + 1]) * double(desc[4 * f + 3]);
+  return total;
+}
+
 int grid_batch_impl(int kind, int prec, int mem, int clamp, int n_frames, const int64_t* desc,
                     const double* pts, const double* x, const double* q, double* out,
                     void* stream) {
@@ -229,7 +266,9 @@ int grid_batch_impl(int kind, int prec, int mem, int clamp, int n_frames, const 
   const int NC = kind == CPETGB_FIELD ? 3 : 1;
 
   GridPlan plan;
-  plan_grid(n_frames, desc, c->sms, plan);
+  int ppt = 4, ips = 8;
+  tuned_grid_shape(prec, kind, grid_pair_evals(n_frames, desc), &ppt, &ips);
+  plan_grid(n_frames, desc, c->sms, plan, ppt, ips);
 
   Scratch S(s);
   const double *dp = pts, *dx = x, *dq = q;
@@ -250,13 +289,13 @@ int grid_batch_impl(int kind, int prec, int mem, int clamp, int n_frames, const 
   CK(h2d(&d_items, S, plan.items.data(), plan.items.size()), "copy work items");
   if (!plan.finals.empty()) {
     CK(h2d(&d_fin, S, plan.finals.data(), plan.finals.size()), "copy split table");
-    CK(S.get(&partial, size_t(plan.n_slots) * kGridTilePts * 3), "alloc partial sums");
+    CK(S.get(&partial, size_t(plan.n_slots) * kGridSlotPts * 3), "alloc partial sums");
   }
   if (reinterpret_cast<uintptr_t>(packed) % 16 != 0)  // bulk async copies need 16-byte sources
     return fail(CPETGB_ECUDA, "scratch allocation is not 16-byte aligned");
   CK(launch_pack_charges(prec, tot_ch, tot_ch, dx, dq, packed, s), "pack charges");
-  CK(launch_grid(prec, kind, clamp ? 1 : 0, static_cast<int>(plan.items.size()), d_items, packed,
-                 dp, dout, partial, c->status, s),
+  CK(launch_grid(prec, kind, clamp ? 1 : 0, ppt, static_cast<int>(plan.items.size()), d_items,
+                 packed, dp, dout, partial, c->status, s),
      "grid kernel launch");
   CK(launch_grid_final(kind, static_cast<int>(plan.finals.size()), d_fin, partial, dout, s),
      "grid reduction launch");
@@ -342,18 +381,23 @@ int topo_impl(int prec, int mem, int L, int N, const double* starts, const int32
   return CPETGB_OK;
 }
 
-int topo_batch_impl(int prec, int mem, int F, const int64_t* desc, const double* params,
-                    const double* starts, const int32_t* n_iter, const double* x, const double* q,
-                    double* result, double* ends, int32_t* steps, void* stream) {
+struct TopoTables {
+  std::vector<TopoFrame> frames;
+  std::vector<int64_t> src;  // per frame {charge offset, charge count} into x/q
+  int64_t tot_lines = 0, tot_ch = 0, packed_elems = 0;
+  int max_res = 0, max_pairs = 0;
+};
+
+// Frame table of a streamline launch: padded sizes, packed offsets (FP32C
+// frames occupy n_pad float4 -- the pair block A then B --, FP64 frames n_pad
+// Charge64), which frames stay resident in shared memory.
+int build_topo_tables(int prec, int F, const int64_t* desc, const double* params, TopoTables& t) {
   if (!valid_prec(prec)) return fail(CPETGB_EINVAL, "bad precision %d", prec);
-  if (!valid_mem(mem)) return fail(CPETGB_EINVAL, "bad memory kind %d", mem);
   if (F < 0 || (F > 0 && (!desc || !params))) return fail(CPETGB_EINVAL, "bad frame table");
   const int pad = topo_charge_pad(prec);
   const size_t res_limit = prec == CPETGB_FP32C ? topo_resident_limit(prec) : 0;
-  std::vector<TopoFrame> frames(F);
-  std::vector<int64_t> src(2 * size_t(F));
-  int64_t tot_lines = 0, tot_ch = 0, packed_elems = 0;
-  int max_res = 0, max_pairs = 0;
+  t.frames.assign(F, TopoFrame{});
+  t.src.assign(2 * size_t(F), 0);
   for (int f = 0; f < F; ++f) {
     const int64_t co = desc[4 * f], n = desc[4 * f + 1], lo = desc[4 * f + 2], L = desc[4 * f + 3];
     if (co < 0 || n < 0 || lo < 0 || L < 0 || n > INT_MAX / 2 || L > INT_MAX)
@@ -363,25 +407,38 @@ int topo_batch_impl(int prec, int mem, int F, const int64_t* desc, const double*
     for (int k = 1; k < 4; ++k)
       if (!std::isfinite(pr[k]) || pr[k] < 0)
         return fail(CPETGB_EINVAL, "frame %d: half-widths must be finite and >= 0", f);
-    TopoFrame& fr = frames[f];
+    TopoFrame& fr = t.frames[f];
     fr.n_pad = static_cast<int32_t>(((std::max<int64_t>(n, 1) + pad - 1) / pad) * pad);
-    fr.packed_off = packed_elems;
-    // FP32C frames occupy n_pad float4 (pair block A then B); FP64 n_pad Charge64
-    packed_elems += fr.n_pad;
+    fr.packed_off = t.packed_elems;
+    t.packed_elems += fr.n_pad;
     fr.line_off = lo;
     fr.n_lines = static_cast<int32_t>(L);
     fr.resident = (prec == CPETGB_FP32C && static_cast<size_t>(fr.n_pad) <= res_limit) ? 1 : 0;
     fr.pad_ = 0;
     fr.step = pr[0];
     for (int k = 0; k < 3; ++k) fr.half[k] = pr[1 + k];
-    if (fr.resident) max_res = std::max(max_res, int(fr.n_pad));
-    max_pairs = std::max(max_pairs, int(fr.n_pad));
-    src[2 * f] = co;
-    src[2 * f + 1] = n;
-    tot_lines = std::max(tot_lines, lo + L);
-    tot_ch = std::max(tot_ch, co + n);
+    if (fr.resident) t.max_res = std::max(t.max_res, int(fr.n_pad));
+    t.max_pairs = std::max(t.max_pairs, int(fr.n_pad));
+    t.src[2 * f] = co;
+    t.src[2 * f + 1] = n;
+    t.tot_lines = std::max(t.tot_lines, lo + L);
+    t.tot_ch = std::max(t.tot_ch, co + n);
   }
-  if (tot_lines > INT_MAX) return fail(CPETGB_EINVAL, "too many lines");
+  if (t.tot_lines > INT_MAX) return fail(CPETGB_EINVAL, "too many lines");
+  return CPETGB_OK;
+}
+
+int topo_batch_impl(int prec, int mem, int F, const int64_t* desc, const double* params,
+                    const double* starts, const int32_t* n_iter, const double* x, const double* q,
+                    double* result, double* ends, int32_t* steps, void* stream) {
+  if (!valid_mem(mem)) return fail(CPETGB_EINVAL, "bad memory kind %d", mem);
+  TopoTables t;
+  int rc0 = build_topo_tables(prec, F, desc, params, t);
+  if (rc0 != CPETGB_OK) return rc0;
+  std::vector<TopoFrame>& frames = t.frames;
+  std::vector<int64_t>& src = t.src;
+  const int64_t tot_lines = t.tot_lines, tot_ch = t.tot_ch, packed_elems = t.packed_elems;
+  const int max_res = t.max_res, max_pairs = t.max_pairs;
   if (tot_lines == 0) return CPETGB_OK;
   if (!starts || !n_iter || !result) return fail(CPETGB_EINVAL, "line pointer is NULL");
   if (tot_ch > 0 && (!x || !q)) return fail(CPETGB_EINVAL, "charge pointer is NULL");
@@ -490,9 +547,210 @@ std::vector<double> widen(const float* p, size_t n) {
   return v;
 }
 
+template <typename T>
+cudaError_t plan_alloc(std::vector<void*>& bufs, T** p, size_t count) {
+  *p = nullptr;
+  void* v = nullptr;
+  cudaError_t e = cudaMalloc(&v, std::max<size_t>(count, 1) * sizeof(T));
+  if (e == cudaSuccess) {
+    bufs.push_back(v);
+    *p = static_cast<T*>(v);
+  }
+  return e;
+}
+
+}  // namespace
+
+// A prepared launch: device tables and scratch allocated once, the launch
+// sequence captured into a CUDA graph and replayed by cpetgb_plan_launch.
+struct cpetgb_plan {
+  int device = -1;
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  std::vector<void*> bufs;
+  ~cpetgb_plan() {
+    if (exec) cudaGraphExecDestroy(exec);
+    if (graph) cudaGraphDestroy(graph);
+    for (void* p : bufs) cudaFree(p);
+  }
+};
+
+namespace {
+
+// Captures `body` (launches on the capture stream) into plan->graph/exec.
+template <typename Body>
+int capture_plan(cpetgb_plan* pl, Body body) {
+  cudaStream_t cs = nullptr;
+  CK(cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking), "capture stream");
+  cudaError_t e = cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal);
+  if (e != cudaSuccess) {
+    cudaStreamDestroy(cs);
+    return cuda_fail(e, "begin capture");
+  }
+  const int rc = body(cs);
+  cudaGraph_t g = nullptr;
+  e = cudaStreamEndCapture(cs, &g);
+  cudaStreamDestroy(cs);
+  if (rc != CPETGB_OK) {
+    if (g) cudaGraphDestroy(g);
+    return rc;
+  }
+  if (e != cudaSuccess) return cuda_fail(e, "end capture");
+  pl->graph = g;
+  CK(cudaGraphInstantiate(&pl->exec, g, 0), "graph instantiate");
+  return CPETGB_OK;
+}
+
+int grid_plan_impl(cpetgb_plan** out_plan, int kind, int prec, int clamp, int n_frames,
+                   const int64_t* desc, const double* pts, const double* x, const double* q,
+                   double* out) {
+  if (!out_plan) return fail(CPETGB_EINVAL, "plan pointer is NULL");
+  *out_plan = nullptr;
+  if (kind != CPETGB_FIELD && kind != CPETGB_ESP) return fail(CPETGB_EINVAL, "bad grid kind %d", kind);
+  if (!valid_prec(prec)) return fail(CPETGB_EINVAL, "bad precision %d", prec);
+  if (n_frames < 0 || (n_frames > 0 && !desc)) return fail(CPETGB_EINVAL, "bad frame table");
+  int64_t tot_pts = 0, tot_ch = 0;
+  for (int f = 0; f < n_frames; ++f) {
+    const int64_t co = desc[4 * f], n = desc[4 * f + 1], po = desc[4 * f + 2], P = desc[4 * f + 3];
+    if (co < 0 || n < 0 || po < 0 || P < 0 || n > INT_MAX || P > INT_MAX)
+      return fail(CPETGB_EINVAL, "frame %d: negative or oversized offset/count", f);
+    tot_pts = std::max(tot_pts, po + P);
+    tot_ch = std::max(tot_ch, co + n);
+  }
+  if (tot_pts > 0 && (!pts || !out)) return fail(CPETGB_EINVAL, "points/output pointer is NULL");
+  if (tot_ch > 0 && (!x || !q)) return fail(CPETGB_EINVAL, "charge pointer is NULL");
+  int rc;
+  Ctx* c = context(&rc);
+  if (!c) return rc;
+  GridPlan gp;
+  int ppt = 4, ips = 8;
+  tuned_grid_shape(prec, kind, grid_pair_evals(n_frames, desc), &ppt, &ips);
+  plan_grid(n_frames, desc, c->sms, gp, ppt, ips);
+  cpetgb_plan* pl = new cpetgb_plan();
+  cudaGetDevice(&pl->device);
+  unsigned char* packed = nullptr;
+  GridItem* d_items = nullptr;
+  GridFinal* d_fin = nullptr;
+  double* partial = nullptr;
+  cudaError_t e = plan_alloc(pl->bufs, &packed, size_t(std::max<int64_t>(tot_ch, 1)) * kGridRecord);
+  if (e == cudaSuccess) e = plan_alloc(pl->bufs, &d_items, gp.items.size());
+  if (e == cudaSuccess && !gp.items.empty())
+    e = cudaMemcpy(d_items, gp.items.data(), gp.items.size() * sizeof(GridItem), cudaMemcpyHostToDevice);
+  if (e == cudaSuccess && !gp.finals.empty()) {
+    e = plan_alloc(pl->bufs, &d_fin, gp.finals.size());
+    if (e == cudaSuccess)
+      e = cudaMemcpy(d_fin, gp.finals.data(), gp.finals.size() * sizeof(GridFinal),
+                     cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = plan_alloc(pl->bufs, &partial, size_t(gp.n_slots) * kGridSlotPts * 3);
+  }
+  if (e != cudaSuccess) {
+    delete pl;
+    return cuda_fail(e, "plan allocation");
+  }
+  const int n_items = static_cast<int>(gp.items.size()), n_fin = static_cast<int>(gp.finals.size());
+  e = preload_grid_kernels(prec, kind, clamp ? 1 : 0, ppt);
+  if (e != cudaSuccess) {
+    delete pl;
+    return cuda_fail(e, "kernel load");
+  }
+  rc = capture_plan(pl, [&](cudaStream_t cs) -> int {
+    CK(launch_pack_charges(prec, tot_ch, tot_ch, x, q, packed, cs), "pack charges");
+    CK(launch_grid(prec, kind, clamp ? 1 : 0, ppt, n_items, d_items, packed, pts, out, partial,
+                   c->status, cs),
+       "grid kernel launch");
+    CK(launch_grid_final(kind, n_fin, d_fin, partial, out, cs), "grid reduction launch");
+    return CPETGB_OK;
+  });
+  if (rc != CPETGB_OK) {
+    delete pl;
+    return rc;
+  }
+  *out_plan = pl;
+  return CPETGB_OK;
+}
+
+int topo_plan_impl(cpetgb_plan** out_plan, int prec, int F, const int64_t* desc,
+                   const double* params, const double* starts, const int32_t* n_iter,
+                   const double* x, const double* q, double* result, double* ends, int32_t* steps) {
+  if (!out_plan) return fail(CPETGB_EINVAL, "plan pointer is NULL");
+  *out_plan = nullptr;
+  TopoTables t;
+  int rc = build_topo_tables(prec, F, desc, params, t);
+  if (rc != CPETGB_OK) return rc;
+  if (t.tot_lines > 0 && (!starts || !n_iter || !result))
+    return fail(CPETGB_EINVAL, "line pointer is NULL");
+  if (t.tot_ch > 0 && (!x || !q)) return fail(CPETGB_EINVAL, "charge pointer is NULL");
+  Ctx* c = context(&rc);
+  if (!c) return rc;
+  cpetgb_plan* pl = new cpetgb_plan();
+  cudaGetDevice(&pl->device);
+  unsigned char* packed = nullptr;
+  TopoFrame* d_frames = nullptr;
+  int64_t* d_src = nullptr;
+  int* queues = nullptr;
+  cudaError_t e =
+      plan_alloc(pl->bufs, &packed, size_t(std::max<int64_t>(t.packed_elems, 1)) * packed_size(prec));
+  if (e == cudaSuccess) e = plan_alloc(pl->bufs, &d_frames, t.frames.size());
+  if (e == cudaSuccess) e = plan_alloc(pl->bufs, &d_src, t.src.size());
+  if (e == cudaSuccess) e = plan_alloc(pl->bufs, &queues, size_t(std::max(F, 1)));
+  if (e == cudaSuccess && F > 0)
+    e = cudaMemcpy(d_frames, t.frames.data(), t.frames.size() * sizeof(TopoFrame),
+                   cudaMemcpyHostToDevice);
+  if (e == cudaSuccess && F > 0)
+    e = cudaMemcpy(d_src, t.src.data(), t.src.size() * sizeof(int64_t), cudaMemcpyHostToDevice);
+  if (e != cudaSuccess) {
+    delete pl;
+    return cuda_fail(e, "plan allocation");
+  }
+  if (reinterpret_cast<uintptr_t>(packed) % 16 != 0) {
+    delete pl;
+    return fail(CPETGB_ECUDA, "plan allocation is not 16-byte aligned");
+  }
+  TopoParams p{};
+  p.n_lines = static_cast<int>(t.tot_lines);
+  p.starts = starts;
+  p.n_iter = n_iter;
+  p.packed = packed;
+  p.result = result;
+  p.ends = ends;
+  p.steps = steps;
+  p.queue = queues;
+  p.status = c->status;
+  p.frames = d_frames;
+  p.n_frames = F;
+  p.max_resident_pad = t.max_res;
+  const int max_pairs = t.max_pairs;
+  rc = capture_plan(pl, [&](cudaStream_t cs) -> int {
+    CK(cudaMemsetAsync(queues, 0, sizeof(int) * size_t(std::max(F, 1)), cs), "zero queues");
+    CK(launch_pack_topo_frames(prec, F, d_frames, d_src, x, q, packed, max_pairs, cs),
+       "pack charges");
+    CK(launch_topo_frames(prec, p, c->sms, cs), "topo kernel launch");
+    return CPETGB_OK;
+  });
+  if (rc != CPETGB_OK) {
+    delete pl;
+    return rc;
+  }
+  *out_plan = pl;
+  return CPETGB_OK;
+}
+
 }  // namespace
 
 int cpetgb::set_error(int code, const char* msg) { return fail(code, "%s", msg); }
+
+int cpetgb::tuned_topo_slots(int prec, bool resident, int n_lines) {
+  const int v = tune_lookup(tune_key(kOpTopo, prec, resident ? 1 : 0, double(n_lines)));
+  return v == 1 ? 2 : 4;
+}
+
+void cpetgb::tuned_grid_shape(int prec, int kind, double pair_evals, int* ppt, int* items_per_sm) {
+  int v = tune_lookup(tune_key(kOpGrid, prec, kind, pair_evals));
+  if (v < 0 || v >= kGridVariants) v = 1;  // untuned: 4 points per thread, 8 items per SM
+  static const int ips[3] = {4, 8, 16};
+  *ppt = (v / 3) == 1 ? 8 : 4;
+  *items_per_sm = ips[v % 3];
+}
 
 extern "C" {
 
@@ -559,6 +817,61 @@ int cpetgb_topo_batch(int precision, int mem, int n_frames, const int64_t* desc,
                       int32_t* steps, void* stream) {
   return topo_batch_impl(precision, mem, n_frames, desc, params, starts, n_iter, x, q, result, ends,
                          steps, stream);
+}
+
+int cpetgb_grid_plan_create(cpetgb_plan** plan, int kind, int precision, int clamp, int n_frames,
+                            const int64_t* desc, const double* points, const double* x,
+                            const double* q, double* out) {
+  return grid_plan_impl(plan, kind, precision, clamp, n_frames, desc, points, x, q, out);
+}
+
+int cpetgb_topo_plan_create(cpetgb_plan** plan, int precision, int n_frames, const int64_t* desc,
+                            const double* params, const double* starts, const int32_t* n_iter,
+                            const double* x, const double* q, double* result, double* ends,
+                            int32_t* steps) {
+  return topo_plan_impl(plan, precision, n_frames, desc, params, starts, n_iter, x, q, result, ends,
+                        steps);
+}
+
+int cpetgb_tune_key(int op, int precision, int cls, double size) {
+  if ((op != kOpGrid && op != kOpTopo) || !valid_prec(precision) || cls < 0 || cls > 15 ||
+      !(size >= 0))
+    return fail(CPETGB_EINVAL, "bad tuning key arguments");
+  return tune_key(op, precision, cls, size);
+}
+
+int cpetgb_tune_variants(int op) {
+  if (op == kOpGrid) return kGridVariants;
+  if (op == kOpTopo) return kTopoVariants;
+  return fail(CPETGB_EINVAL, "bad operation %d", op);
+}
+
+int cpetgb_tune_set(int key, int variant) {
+  const int op = key >> 12;
+  const int n = op == kOpGrid ? kGridVariants : (op == kOpTopo ? kTopoVariants : 0);
+  if (key < 0 || variant < -1 || variant >= n) return fail(CPETGB_EINVAL, "bad tuning entry");
+  std::lock_guard<std::mutex> lock(g_tune_mu);
+  if (variant < 0)
+    g_tune.erase(key);
+  else
+    g_tune[key] = variant;
+  return CPETGB_OK;
+}
+
+int cpetgb_tune_get(int key) { return tune_lookup(key); }
+
+int cpetgb_plan_launch(cpetgb_plan* plan, void* stream) {
+  if (!plan || !plan->exec) return fail(CPETGB_EINVAL, "plan is NULL or empty");
+  int dev = -1;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev != plan->device)
+    return fail(CPETGB_EINVAL, "plan belongs to device %d; current device is %d", plan->device, dev);
+  CK(cudaGraphLaunch(plan->exec, static_cast<cudaStream_t>(stream)), "graph launch");
+  return CPETGB_OK;
+}
+
+int cpetgb_plan_destroy(cpetgb_plan* plan) {
+  delete plan;
+  return CPETGB_OK;
 }
 
 int cpetgb_topo_hist2d(int mem, int n_lines, const double* result, int nb_dist, int nb_curv,

@@ -5,12 +5,12 @@
 // a point) and calc_esp_base (math_module.c:453-486, potential), which the
 // reference evaluates one point at a time on one CPU core.
 //
-// Work decomposition: a CTA owns one GridItem = a tile of kGridTilePts points
-// of one frame (kGridPPT points per thread, kept in registers) and a contiguous
+// Work decomposition: a CTA owns one GridItem = a tile of kGridSlotPts points
+// of one frame (PPT points per thread, kept in registers) and a contiguous
 // range of that frame's charges.  The charges stream through a ring of shared
 // memory stages filled by 1-D bulk async copies (cp.async.bulk) that complete
 // on mbarriers; every thread reads each staged charge as a broadcast and
-// applies it to its kGridPPT points.
+// applies it to its PPT points.
 //
 // Precision forms:
 //   FP32C  pair terms in FP32 with the MUFU rsqrt; each stage's contribution is
@@ -76,24 +76,26 @@ __device__ __forceinline__ void kahan_add2(uint64_t& s, uint64_t& c, uint64_t t)
 
 constexpr int kKahanRun = 16;  // FP32C: charges summed plainly between Kahan steps
 
-// FP32C body: this thread's 4 points as two packed pairs (points k = 2g, 2g+1).
-template <int KIND, bool CLAMP>
+// FP32C body: this thread's points as G packed pairs (points k = 2g, 2g+1).
+template <int KIND, bool CLAMP, int G>
 __device__ __forceinline__ void grid_tile_f32x2(const ChargeDup* __restrict__ tl, int cnt,
-                                                const uint64_t (&px)[2], const uint64_t (&py)[2],
-                                                const uint64_t (&pz)[2], uint64_t (&acc)[3][2],
-                                                uint64_t (&cmp)[3][2]) {
+                                                const uint64_t (&px)[G], const uint64_t (&py)[G],
+                                                const uint64_t (&pz)[G], uint64_t (&acc)[3][G],
+                                                uint64_t (&cmp)[3][G]) {
   constexpr int NC = (KIND == kField) ? 3 : 1;
   for (int j0 = 0; j0 < cnt; j0 += kKahanRun) {
     const int j1 = min(cnt, j0 + kKahanRun);
-    uint64_t part[NC][2];
+    uint64_t part[NC][G];
 #pragma unroll
-    for (int c = 0; c < NC; ++c) part[c][0] = part[c][1] = 0ull;
+    for (int c = 0; c < NC; ++c)
+#pragma unroll
+      for (int g = 0; g < G; ++g) part[c][g] = 0ull;
 #pragma unroll 4
     for (int j = j0; j < j1; ++j) {
       const ulonglong2 xy = tl[j].xy;
       const ulonglong2 zq = tl[j].zq;
 #pragma unroll
-      for (int g = 0; g < 2; ++g) {
+      for (int g = 0; g < G; ++g) {
         const uint64_t dx = sub2(px[g], xy.x);
         const uint64_t dy = sub2(py[g], xy.y);
         const uint64_t dz = sub2(pz[g], zq.x);
@@ -117,11 +119,11 @@ __device__ __forceinline__ void grid_tile_f32x2(const ChargeDup* __restrict__ tl
 #pragma unroll
     for (int c = 0; c < NC; ++c)
 #pragma unroll
-      for (int g = 0; g < 2; ++g) kahan_add2(acc[c][g], cmp[c][g], part[c][g]);
+      for (int g = 0; g < G; ++g) kahan_add2(acc[c][g], cmp[c][g], part[c][g]);
   }
 }
 
-template <int PREC, int KIND, bool CLAMP>
+template <int PREC, int KIND, bool CLAMP, int PPT>
 __global__ void __launch_bounds__(kGridThreads)
     grid_kernel(const GridItem* __restrict__ items, const void* __restrict__ packed,
                 const double* __restrict__ points, double* __restrict__ out,
@@ -159,9 +161,9 @@ __global__ void __launch_bounds__(kGridThreads)
   }
 
   // This thread's points, in registers (FP32C: packed in pairs).
-  Real px[kGridPPT], py[kGridPPT], pz[kGridPPT];
+  Real px[PPT], py[PPT], pz[PPT];
 #pragma unroll
-  for (int k = 0; k < kGridPPT; ++k) {
+  for (int k = 0; k < PPT; ++k) {
     const int pl = tid + k * kGridThreads;
     if (pl < it.p_count) {
       const double* pp = points + 3 * (it.point_off + it.p_begin + pl);
@@ -172,10 +174,11 @@ __global__ void __launch_bounds__(kGridThreads)
       px[k] = py[k] = pz[k] = static_cast<Real>(1.0e4);  // far away, never written
     }
   }
-  [[maybe_unused]] uint64_t px2[2], py2[2], pz2[2], acc2[3][2], cmp2[3][2];
+  constexpr int G = PPT / 2;
+  [[maybe_unused]] uint64_t px2[G], py2[G], pz2[G], acc2[3][G], cmp2[3][G];
   if constexpr (PREC == kFP32C) {
 #pragma unroll
-    for (int g = 0; g < 2; ++g) {
+    for (int g = 0; g < G; ++g) {
       px2[g] = pk2(px[2 * g], px[2 * g + 1]);
       py2[g] = pk2(py[2 * g], py[2 * g + 1]);
       pz2[g] = pk2(pz[2 * g], pz[2 * g + 1]);
@@ -185,11 +188,11 @@ __global__ void __launch_bounds__(kGridThreads)
   }
 
   // FP64 running sums.
-  Real acc[NC][kGridPPT];
+  Real acc[NC][PPT];
 #pragma unroll
   for (int c = 0; c < NC; ++c)
 #pragma unroll
-    for (int k = 0; k < kGridPPT; ++k) acc[c][k] = Real(0);
+    for (int k = 0; k < PPT; ++k) acc[c][k] = Real(0);
 
   bool ok = true;
   for (int t = 0; t < n_tiles; ++t) {
@@ -202,18 +205,18 @@ __global__ void __launch_bounds__(kGridThreads)
     const int cnt = min(TC, n - t * TC);
     const ChargeT* tl = &tile[s][0];
     if constexpr (PREC == kFP32C) {
-      grid_tile_f32x2<KIND, CLAMP>(tl, cnt, px2, py2, pz2, acc2, cmp2);
+      grid_tile_f32x2<KIND, CLAMP, G>(tl, cnt, px2, py2, pz2, acc2, cmp2);
     } else {
-      Real part[NC][kGridPPT];
+      Real part[NC][PPT];
 #pragma unroll
       for (int c = 0; c < NC; ++c)
 #pragma unroll
-        for (int k = 0; k < kGridPPT; ++k) part[c][k] = Real(0);
+        for (int k = 0; k < PPT; ++k) part[c][k] = Real(0);
 #pragma unroll 4
       for (int j = 0; j < cnt; ++j) {
         const ChargeT ch = tl[j];
 #pragma unroll
-        for (int k = 0; k < kGridPPT; ++k) {
+        for (int k = 0; k < PPT; ++k) {
           const Real dx = px[k] - ch.x;
           const Real dy = py[k] - ch.y;
           const Real dz = pz[k] - ch.z;
@@ -233,13 +236,13 @@ __global__ void __launch_bounds__(kGridThreads)
 #pragma unroll
       for (int c = 0; c < NC; ++c)
 #pragma unroll
-        for (int k = 0; k < kGridPPT; ++k) acc[c][k] += part[c][k];
+        for (int k = 0; k < PPT; ++k) acc[c][k] += part[c][k];
     }
   }
   if (!ok) return;
 
 #pragma unroll
-  for (int k = 0; k < kGridPPT; ++k) {
+  for (int k = 0; k < PPT; ++k) {
     const int pl = tid + k * kGridThreads;
     if (pl >= it.p_count) continue;
 #pragma unroll
@@ -257,7 +260,7 @@ __global__ void __launch_bounds__(kGridThreads)
       if (it.slot < 0) {
         out[NC * (it.point_off + it.p_begin + pl) + c] = v;
       } else {
-        partial[(static_cast<int64_t>(it.slot) * kGridTilePts + pl) * 3 + c] = v;
+        partial[(static_cast<int64_t>(it.slot) * kGridSlotPts + pl) * 3 + c] = v;
       }
     }
   }
@@ -272,7 +275,7 @@ __global__ void grid_final_kernel(const GridFinal* __restrict__ fin,
     const int pl = i / NC, c = i % NC;
     double v = 0.0;
     for (int s = 0; s < f.n_split; ++s)
-      v += partial[(static_cast<int64_t>(f.slot_base + s) * kGridTilePts + pl) * 3 + c];
+      v += partial[(static_cast<int64_t>(f.slot_base + s) * kGridSlotPts + pl) * 3 + c];
     out[NC * (f.out_row + pl) + c] = v;
   }
 }
@@ -313,17 +316,34 @@ __global__ void pack_f64_kernel(int64_t n, int64_t n_pad, const double* __restri
   }
 }
 
-template <int PREC, int KIND>
+template <int PREC, int KIND, int PPT>
 cudaError_t launch_grid_t(int clamp, int n_items, const GridItem* items, const void* packed,
                           const double* points, double* out, double* partial, int* status,
                           cudaStream_t s) {
   if (clamp)
-    grid_kernel<PREC, KIND, true>
+    grid_kernel<PREC, KIND, true, PPT>
         <<<n_items, kGridThreads, 0, s>>>(items, packed, points, out, partial, status);
   else
-    grid_kernel<PREC, KIND, false>
+    grid_kernel<PREC, KIND, false, PPT>
         <<<n_items, kGridThreads, 0, s>>>(items, packed, points, out, partial, status);
   return cudaGetLastError();
+}
+
+template <int PREC, int KIND>
+cudaError_t launch_grid_p(int clamp, int ppt, int n_items, const GridItem* items,
+                          const void* packed, const double* points, double* out, double* partial,
+                          int* status, cudaStream_t s) {
+  return ppt == 8 ? launch_grid_t<PREC, KIND, 8>(clamp, n_items, items, packed, points, out,
+                                                 partial, status, s)
+                  : launch_grid_t<PREC, KIND, 4>(clamp, n_items, items, packed, points, out,
+                                                 partial, status, s);
+}
+
+template <int PREC, int KIND, int PPT>
+cudaError_t preload_t(int clamp) {
+  cudaFuncAttributes a;
+  return clamp ? cudaFuncGetAttributes(&a, grid_kernel<PREC, KIND, true, PPT>)
+               : cudaFuncGetAttributes(&a, grid_kernel<PREC, KIND, false, PPT>);
 }
 
 }  // namespace
@@ -339,20 +359,42 @@ cudaError_t launch_pack_charges(int prec, int64_t n, int64_t n_pad, const double
   return cudaGetLastError();
 }
 
-cudaError_t launch_grid(int prec, int kind, int clamp, int n_items, const GridItem* items,
+cudaError_t launch_grid(int prec, int kind, int clamp, int ppt, int n_items, const GridItem* items,
                         const void* packed, const double* points, double* out, double* partial,
                         int* status, cudaStream_t s) {
   if (n_items <= 0) return cudaSuccess;
   if (prec == kFP32C) {
-    return kind == kField ? launch_grid_t<kFP32C, kField>(clamp, n_items, items, packed, points,
+    return kind == kField ? launch_grid_p<kFP32C, kField>(clamp, ppt, n_items, items, packed, points,
                                                          out, partial, status, s)
-                          : launch_grid_t<kFP32C, kEsp>(0, n_items, items, packed, points, out,
+                          : launch_grid_p<kFP32C, kEsp>(0, ppt, n_items, items, packed, points, out,
                                                        partial, status, s);
   }
-  return kind == kField ? launch_grid_t<kFP64, kField>(clamp, n_items, items, packed, points, out,
-                                                      partial, status, s)
-                        : launch_grid_t<kFP64, kEsp>(0, n_items, items, packed, points, out,
+  return kind == kField ? launch_grid_p<kFP64, kField>(clamp, ppt, n_items, items, packed, points,
+                                                      out, partial, status, s)
+                        : launch_grid_p<kFP64, kEsp>(0, ppt, n_items, items, packed, points, out,
                                                     partial, status, s);
+}
+
+cudaError_t preload_grid_kernels(int prec, int kind, int clamp, int ppt) {
+  cudaError_t e;
+  if (prec == kFP32C) {
+    if (kind == kField)
+      e = ppt == 8 ? preload_t<kFP32C, kField, 8>(clamp) : preload_t<kFP32C, kField, 4>(clamp);
+    else
+      e = ppt == 8 ? preload_t<kFP32C, kEsp, 8>(0) : preload_t<kFP32C, kEsp, 4>(0);
+  } else {
+    if (kind == kField)
+      e = ppt == 8 ? preload_t<kFP64, kField, 8>(clamp) : preload_t<kFP64, kField, 4>(clamp);
+    else
+      e = ppt == 8 ? preload_t<kFP64, kEsp, 8>(0) : preload_t<kFP64, kEsp, 4>(0);
+  }
+  if (e != cudaSuccess) return e;
+  cudaFuncAttributes a;
+  e = kind == kField ? cudaFuncGetAttributes(&a, grid_final_kernel<kField>)
+                     : cudaFuncGetAttributes(&a, grid_final_kernel<kEsp>);
+  if (e != cudaSuccess) return e;
+  return prec == kFP32C ? cudaFuncGetAttributes(&a, pack_dup_f32_kernel)
+                        : cudaFuncGetAttributes(&a, pack_f64_kernel);
 }
 
 cudaError_t launch_grid_final(int kind, int n_final, const GridFinal* fin, const double* partial,

@@ -32,7 +32,7 @@ struct GridItem {
   int64_t charge_off;  // first packed charge of the frame
   int64_t point_off;   // first point of the frame (points / output rows)
   int32_t p_begin;     // first point of this tile inside the frame
-  int32_t p_count;     // points in this tile (<= kGridTilePts)
+  int32_t p_count;     // points in this tile (<= kGridThreads * points per thread)
   int32_t n_begin;     // first charge of this item inside the frame
   int32_t n_count;     // charges of this item
   int32_t slot;        // partial-sum slot (>= 0), or -1 to write the final value
@@ -51,8 +51,8 @@ struct GridFinal {
 static_assert(sizeof(GridFinal) == 24, "GridFinal layout");
 
 constexpr int kGridThreads = 128;
-constexpr int kGridPPT = 4;  // points per thread
-constexpr int kGridTilePts = kGridThreads * kGridPPT;
+constexpr int kGridMaxPPT = 8;                              // points per thread: 4 or 8
+constexpr int kGridSlotPts = kGridThreads * kGridMaxPPT;    // stride of a partial-sum slot
 
 // grid.cu
 // Packs x[n][3], q[n] for the grid kernels (32-byte records: Charge64, or the
@@ -60,9 +60,11 @@ constexpr int kGridTilePts = kGridThreads * kGridPPT;
 // charges placed far outside any box (they contribute exactly zero).
 cudaError_t launch_pack_charges(int prec, int64_t n, int64_t n_pad, const double* x,
                                 const double* q, void* packed, cudaStream_t s);
-cudaError_t launch_grid(int prec, int kind, int clamp, int n_items, const GridItem* items,
+cudaError_t launch_grid(int prec, int kind, int clamp, int ppt, int n_items, const GridItem* items,
                         const void* packed, const double* points, double* out,
                         double* partial, int* status, cudaStream_t s);
+// Loads the module code of the grid kernels (before a graph capture).
+cudaError_t preload_grid_kernels(int prec, int kind, int clamp, int ppt);
 cudaError_t launch_grid_final(int kind, int n_final, const GridFinal* fin,
                               const double* partial, double* out, cudaStream_t s);
 
@@ -114,6 +116,10 @@ cudaError_t launch_pack_topo(int prec, int64_t n, int64_t n_pad, const double* x
 
 // api.cu: records `msg` as the calling thread's last error and returns `code`.
 int set_error(int code, const char* msg);
+
+// api.cu: the tuned variants (autotuner table, defaults when untuned).
+int tuned_topo_slots(int prec, bool resident, int n_lines);    // 2 or 4 line slots per warp
+void tuned_grid_shape(int prec, int kind, double pair_evals, int* ppt, int* items_per_sm);
 
 // hist.cu
 cudaError_t launch_hist2d(int n, const double* vals, int nb0, int nb1, const double* range,

@@ -48,7 +48,7 @@ constexpr int kTopoWarps = kTopoThreads / 32;
 constexpr int kLanePairs = 16;                  // charge pairs per lane between Kahan steps
 constexpr int kChargePad32 = 32 * kLanePairs * 2;  // FP32C frames: multiple of 1024 charges
 constexpr int kChargePad64 = 256;               // FP64 frames
-constexpr int kSlots = 4;                       // line slots per warp
+// Line slots per warp S (template parameter): 4 (default) or 2.
 
 enum Phase : int { kMain = 0, kStart1 = 1, kStart2 = 2, kEnd1 = 3, kEnd2 = 4 };
 
@@ -202,10 +202,10 @@ __device__ bool slot_advance(Slot& sl, SlotRec& rec, const double nx[3], const T
 // a ready operand of the packed f32x2 instructions: one instruction evaluates
 // a pair term for two charges.  Lanes take pairs lane-strided; every
 // kLanePairs pairs the two packed streams are added and Kahan-accumulated.
-template <int NA>
+template <int NA, int S>
 __device__ __forceinline__ void sweep_f32x2(const ulonglong2* __restrict__ A,
                                             const ulonglong2* __restrict__ B, int n_pairs,
-                                            int lane, const uint64_t (&ex2)[kSlots][3],
+                                            int lane, const uint64_t (&ex2)[S][3],
                                             float& total) {
   float acc[NA][3], cmp[NA][3];
 #pragma unroll
@@ -245,19 +245,21 @@ __device__ __forceinline__ void sweep_f32x2(const ulonglong2* __restrict__ A,
         kahan_add(acc[e][c], cmp[e][c], __fadd_rn(lo, hi2));
       }
   }
-  // Lane partials (acc - cmp, unevaluated pairs) as 16 values v = 3e + c,
+  // Lane partials (acc - cmp, unevaluated pairs) as NV = 4S values v = 3e + c,
   // reduced across the warp by a reduce-scatter of error-free pair additions:
-  // each level halves the values a lane keeps; afterwards lanes 2v and 2v+1
-  // hold the total of value v.
-  float h[16], l[16];
+  // each of the LV levels halves the values a lane keeps, a butterfly finishes;
+  // afterwards the lanes with (lane >> (5 - LV)) == v hold the total of value v.
+  constexpr int NV = 4 * S;
+  constexpr int LV = (S == 4) ? 4 : 3;
+  float h[NV], l[NV];
 #pragma unroll
-  for (int v = 0; v < 16; ++v) {
+  for (int v = 0; v < NV; ++v) {
     const int e = v / 3, c = v % 3;
     h[v] = (e < NA) ? acc[e < NA ? e : 0][c] : 0.f;
     l[v] = (e < NA) ? -cmp[e < NA ? e : 0][c] : 0.f;
   }
 #pragma unroll
-  for (int lvl = 0, half = 8; lvl < 4; ++lvl, half >>= 1) {
+  for (int lvl = 0, half = NV / 2; lvl < LV; ++lvl, half >>= 1) {
     const int off = 16 >> lvl;
     const bool upper = (lane & off) != 0;
 #pragma unroll
@@ -273,18 +275,19 @@ __device__ __forceinline__ void sweep_f32x2(const ulonglong2* __restrict__ A,
       pair_add(h[j], l[j], rh, rl);
     }
   }
-  {
-    const float rh = __shfl_xor_sync(0xffffffffu, h[0], 1);
-    const float rl = __shfl_xor_sync(0xffffffffu, l[0], 1);
+#pragma unroll
+  for (int off = 16 >> LV; off >= 1; off >>= 1) {
+    const float rh = __shfl_xor_sync(0xffffffffu, h[0], off);
+    const float rl = __shfl_xor_sync(0xffffffffu, l[0], off);
     pair_add(h[0], l[0], rh, rl);
   }
   total = h[0];
 }
 
 // FP64: charges from global memory (padded with zero charges far away).
-template <int NA>
+template <int NA, int S>
 __device__ __forceinline__ void sweep_f64(const Charge64* __restrict__ g, int n_pad, int lane,
-                                          const double (&ex)[kSlots][3], double (&E)[kSlots][3]) {
+                                          const double (&ex)[S][3], double (&E)[S][3]) {
   double acc[NA][3];
 #pragma unroll
   for (int e = 0; e < NA; ++e)
@@ -324,7 +327,7 @@ __device__ __forceinline__ void sweep_f64(const Charge64* __restrict__ g, int n_
 // One line slot set per warp; processes the lines of frame `fc` (charge
 // arrays chA/chB in the FP32C pair layout, or g in Charge64) until the frame's
 // queue is exhausted and the warp's slots are drained.
-template <int PREC>
+template <int PREC, int S>
 __device__ __forceinline__ void run_frame(const TopoParams& p, const FrameCtx& fc, int* queue,
                                           const ulonglong2* chA, const ulonglong2* chB,
                                           const ulonglong2* smA, const ulonglong2* smB,
@@ -335,21 +338,21 @@ __device__ __forceinline__ void run_frame(const TopoParams& p, const FrameCtx& f
   sl.steps = sl.cap = 0;
   sl.pos[0] = sl.pos[1] = sl.pos[2] = 0.0;
   sl.posf[0] = sl.posf[1] = sl.posf[2] = 0.f;
-  if (lane < kSlots) {
+  if (lane < S) {
     const int li = atomicAdd(queue, 1);
     slot_load(sl, *my_rec, li < fc.n_lines ? static_cast<int>(fc.line_off + li) : -1, p);
   }
   for (;;) {
-    const unsigned active = __ballot_sync(0xffffffffu, lane < kSlots && sl.line >= 0);
+    const unsigned active = __ballot_sync(0xffffffffu, lane < S && sl.line >= 0);
     const int na = __popc(active);
     if (na == 0) break;
     // owner lane of each active slot, in order; this lane's rank among them
-    int src_of[kSlots];
+    int src_of[S];
     int my_rank = -1;
     {
       unsigned m = active;
 #pragma unroll
-      for (int e = 0; e < kSlots; ++e) {
+      for (int e = 0; e < S; ++e) {
         src_of[e] = m ? (__ffs(m) - 1) : 0;
         if (m) m &= m - 1;
         if (src_of[e] == lane && e < na) my_rank = e;
@@ -358,9 +361,9 @@ __device__ __forceinline__ void run_frame(const TopoParams& p, const FrameCtx& f
 
     double nx[3];
     if constexpr (PREC == kFP32C) {
-      uint64_t ex2[kSlots][3];
+      uint64_t ex2[S][3];
 #pragma unroll
-      for (int e = 0; e < kSlots; ++e)
+      for (int e = 0; e < S; ++e)
 #pragma unroll
         for (int c = 0; c < 3; ++c) {
           const float v = __shfl_sync(0xffffffffu, sl.posf[c], src_of[e]);
@@ -370,24 +373,25 @@ __device__ __forceinline__ void run_frame(const TopoParams& p, const FrameCtx& f
       const int n_pairs = n_pad / 2;
       if (resident) {
         switch (na) {
-          case 1: sweep_f32x2<1>(smA, smB, n_pairs, lane, ex2, total); break;
-          case 2: sweep_f32x2<2>(smA, smB, n_pairs, lane, ex2, total); break;
-          case 3: sweep_f32x2<3>(smA, smB, n_pairs, lane, ex2, total); break;
-          default: sweep_f32x2<4>(smA, smB, n_pairs, lane, ex2, total); break;
+          case 1: sweep_f32x2<1, S>(smA, smB, n_pairs, lane, ex2, total); break;
+          case 2: sweep_f32x2<2, S>(smA, smB, n_pairs, lane, ex2, total); break;
+          case 3: sweep_f32x2<(S > 2 ? 3 : 2), S>(smA, smB, n_pairs, lane, ex2, total); break;
+          default: sweep_f32x2<S, S>(smA, smB, n_pairs, lane, ex2, total); break;
         }
       } else {
         switch (na) {
-          case 1: sweep_f32x2<1>(chA, chB, n_pairs, lane, ex2, total); break;
-          case 2: sweep_f32x2<2>(chA, chB, n_pairs, lane, ex2, total); break;
-          case 3: sweep_f32x2<3>(chA, chB, n_pairs, lane, ex2, total); break;
-          default: sweep_f32x2<4>(chA, chB, n_pairs, lane, ex2, total); break;
+          case 1: sweep_f32x2<1, S>(chA, chB, n_pairs, lane, ex2, total); break;
+          case 2: sweep_f32x2<2, S>(chA, chB, n_pairs, lane, ex2, total); break;
+          case 3: sweep_f32x2<(S > 2 ? 3 : 2), S>(chA, chB, n_pairs, lane, ex2, total); break;
+          default: sweep_f32x2<S, S>(chA, chB, n_pairs, lane, ex2, total); break;
         }
       }
-      // component c of slot rank e sits in lanes 2(3e + c), 2(3e + c) + 1
+      // component c of slot rank e sits in lanes (3e + c) << (5 - LV) and up
       float Ef[3];
       const int rk = my_rank >= 0 ? my_rank : 0;
 #pragma unroll
-      for (int c = 0; c < 3; ++c) Ef[c] = __shfl_sync(0xffffffffu, total, 2 * (3 * rk + c));
+      for (int c = 0; c < 3; ++c)
+        Ef[c] = __shfl_sync(0xffffffffu, total, (3 * rk + c) << (S == 4 ? 1 : 2));
       if (my_rank >= 0) {
         // step vector in FP32 (the factor k does not change the direction)
         const float n2 = __fmaf_rn(Ef[0], Ef[0], __fmaf_rn(Ef[1], Ef[1], __fmul_rn(Ef[2], Ef[2])));
@@ -396,23 +400,23 @@ __device__ __forceinline__ void run_frame(const TopoParams& p, const FrameCtx& f
         for (int c = 0; c < 3; ++c) nx[c] = sl.pos[c] + static_cast<double>(__fmul_rn(Ef[c], s));
       }
     } else {
-      double ex[kSlots][3];
+      double ex[S][3];
 #pragma unroll
-      for (int e = 0; e < kSlots; ++e)
+      for (int e = 0; e < S; ++e)
 #pragma unroll
         for (int c = 0; c < 3; ++c) ex[e][c] = __shfl_sync(0xffffffffu, sl.pos[c], src_of[e]);
-      double Es[kSlots][3];
+      double Es[S][3];
       const Charge64* g = reinterpret_cast<const Charge64*>(chA);
       switch (na) {
-        case 1: sweep_f64<1>(g, n_pad, lane, ex, Es); break;
-        case 2: sweep_f64<2>(g, n_pad, lane, ex, Es); break;
-        case 3: sweep_f64<3>(g, n_pad, lane, ex, Es); break;
-        default: sweep_f64<4>(g, n_pad, lane, ex, Es); break;
+        case 1: sweep_f64<1, S>(g, n_pad, lane, ex, Es); break;
+        case 2: sweep_f64<2, S>(g, n_pad, lane, ex, Es); break;
+        case 3: sweep_f64<(S > 2 ? 3 : 2), S>(g, n_pad, lane, ex, Es); break;
+        default: sweep_f64<S, S>(g, n_pad, lane, ex, Es); break;
       }
       if (my_rank >= 0) {
         double E[3] = {0.0, 0.0, 0.0};
 #pragma unroll
-        for (int e = 0; e < kSlots; ++e)
+        for (int e = 0; e < S; ++e)
           if (e == my_rank)
 #pragma unroll
             for (int c = 0; c < 3; ++c) E[c] = Es[e][c];
@@ -436,17 +440,17 @@ __device__ __forceinline__ void run_frame(const TopoParams& p, const FrameCtx& f
 // queue lasts, then moves on (after its own warps are done, so the shared
 // copy of the charges can be replaced).  Frames thus overlap only at their
 // tails and every frame switch costs a CTA one line's latency at most.
-template <int PREC, bool CAN_RESIDE>
+template <int PREC, bool CAN_RESIDE, int S>
 __global__ void __launch_bounds__(kTopoThreads, 1) topo_kernel(TopoParams p, TopoFrame frame0) {
   extern __shared__ __align__(128) unsigned char smem_raw[];
   __shared__ int s_skip;
   const int lane = threadIdx.x & 31;
   const int warp = threadIdx.x >> 5;
-  SlotRec* recs = reinterpret_cast<SlotRec*>(smem_raw);  // [kTopoWarps][kSlots]
-  const size_t rec_bytes = sizeof(SlotRec) * kTopoWarps * kSlots;
+  SlotRec* recs = reinterpret_cast<SlotRec*>(smem_raw);  // [kTopoWarps][S]
+  const size_t rec_bytes = sizeof(SlotRec) * kTopoWarps * S;
   uint64_t* bar = reinterpret_cast<uint64_t*>(smem_raw + rec_bytes);
   ulonglong2* sm_ch = reinterpret_cast<ulonglong2*>(smem_raw + rec_bytes + 128);
-  SlotRec* my_rec = recs + warp * kSlots + (lane < kSlots ? lane : 0);
+  SlotRec* my_rec = recs + warp * S + (lane < S ? lane : 0);
   const int n_frames = p.frames ? p.n_frames : 1;
   uint32_t load_parity = 0;
   if (CAN_RESIDE && threadIdx.x == 0) {
@@ -488,7 +492,7 @@ __global__ void __launch_bounds__(kTopoThreads, 1) topo_kernel(TopoParams p, Top
     const ulonglong2* gA = reinterpret_cast<const ulonglong2*>(
         static_cast<const char*>(p.packed) + fr.packed_off * elem);
     const ulonglong2* gB = gA + fr.n_pad / 2;
-    run_frame<PREC>(p, fc, queue, gA, gB, sm_ch, sm_ch + fr.n_pad / 2, resident, fr.n_pad, my_rec,
+    run_frame<PREC, S>(p, fc, queue, gA, gB, sm_ch, sm_ch + fr.n_pad / 2, resident, fr.n_pad, my_rec,
                     lane);
   }
 }
@@ -517,26 +521,26 @@ __global__ void pack_pairs_kernel(int64_t n, int64_t n_pad, const double* __rest
   }
 }
 
-size_t topo_smem_bytes(int max_resident_pad) {
-  return sizeof(SlotRec) * kTopoWarps * kSlots + 128 + static_cast<size_t>(max_resident_pad) * 16;
+size_t topo_smem_bytes(int S, int max_resident_pad) {
+  return sizeof(SlotRec) * kTopoWarps * S + 128 + static_cast<size_t>(max_resident_pad) * 16;
 }
 
-template <int PREC, bool CAN_RESIDE>
+template <int PREC, bool CAN_RESIDE, int S>
 cudaError_t launch_topo_t(const TopoParams& p, const TopoFrame& f0, int total_lines, int num_sms,
                           cudaStream_t s) {
-  const size_t smem = topo_smem_bytes(CAN_RESIDE ? p.max_resident_pad : 0);
-  cudaError_t err = cudaFuncSetAttribute(topo_kernel<PREC, CAN_RESIDE>,
+  const size_t smem = topo_smem_bytes(S, CAN_RESIDE ? p.max_resident_pad : 0);
+  cudaError_t err = cudaFuncSetAttribute(topo_kernel<PREC, CAN_RESIDE, S>,
                                          cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          static_cast<int>(smem));
   if (err != cudaSuccess) return err;
   int per_sm = 1;
-  err = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, topo_kernel<PREC, CAN_RESIDE>,
+  err = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, topo_kernel<PREC, CAN_RESIDE, S>,
                                                       kTopoThreads, smem);
   if (err != cudaSuccess) return err;
   per_sm = std::max(per_sm, 1);
-  const int max_useful = (total_lines + kTopoWarps * kSlots - 1) / (kTopoWarps * kSlots);
+  const int max_useful = (total_lines + kTopoWarps * S - 1) / (kTopoWarps * S);
   const int grid = std::max(1, std::min(num_sms * per_sm, max_useful));
-  topo_kernel<PREC, CAN_RESIDE><<<grid, kTopoThreads, smem, s>>>(p, f0);
+  topo_kernel<PREC, CAN_RESIDE, S><<<grid, kTopoThreads, smem, s>>>(p, f0);
   return cudaGetLastError();
 }
 
@@ -598,7 +602,7 @@ size_t topo_resident_limit(int prec) {
   int dev = 0, optin = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
-  const size_t fixed = topo_smem_bytes(0) + 256;  // + static shared memory
+  const size_t fixed = topo_smem_bytes(4, 0) + 256;  // + static shared memory
   if (optin <= static_cast<int>(fixed)) return 0;
   size_t n = (static_cast<size_t>(optin) - fixed) / 16;
   return (n / kChargePad32) * kChargePad32;
@@ -622,6 +626,13 @@ cudaError_t launch_pack_topo_frames(int prec, int n_frames, const TopoFrame* d_f
   return cudaGetLastError();
 }
 
+template <int PREC, bool CAN_RESIDE>
+cudaError_t launch_topo_s(const TopoParams& p, const TopoFrame& f0, int total_lines, int num_sms,
+                          cudaStream_t s, int slots) {
+  return slots == 2 ? launch_topo_t<PREC, CAN_RESIDE, 2>(p, f0, total_lines, num_sms, s)
+                    : launch_topo_t<PREC, CAN_RESIDE, 4>(p, f0, total_lines, num_sms, s);
+}
+
 // Single frame: p.packed holds round_up(n_charges, topo_charge_pad(prec)) charges
 // packed by launch_pack_topo (the tail being zero charges far from the box).
 cudaError_t launch_topo(int prec, const TopoParams& p_in, int num_sms, cudaStream_t s) {
@@ -640,17 +651,20 @@ cudaError_t launch_topo(int prec, const TopoParams& p_in, int num_sms, cudaStrea
   p.frames = nullptr;
   p.n_frames = 1;
   p.max_resident_pad = f0.resident ? f0.n_pad : 0;
-  if (prec == kFP64) return launch_topo_t<kFP64, false>(p, f0, p.n_lines, num_sms, s);
-  if (f0.resident) return launch_topo_t<kFP32C, true>(p, f0, p.n_lines, num_sms, s);
-  return launch_topo_t<kFP32C, false>(p, f0, p.n_lines, num_sms, s);
+  const int slots = tuned_topo_slots(prec, f0.resident, p.n_lines);
+  if (prec == kFP64) return launch_topo_s<kFP64, false>(p, f0, p.n_lines, num_sms, s, slots);
+  if (f0.resident) return launch_topo_s<kFP32C, true>(p, f0, p.n_lines, num_sms, s, slots);
+  return launch_topo_s<kFP32C, false>(p, f0, p.n_lines, num_sms, s, slots);
 }
 
 cudaError_t launch_topo_frames(int prec, const TopoParams& p, int num_sms, cudaStream_t s) {
   if (p.n_frames <= 0 || p.n_lines <= 0) return cudaSuccess;
   TopoFrame dummy{};
-  if (prec == kFP64) return launch_topo_t<kFP64, false>(p, dummy, p.n_lines, num_sms, s);
-  if (p.max_resident_pad > 0) return launch_topo_t<kFP32C, true>(p, dummy, p.n_lines, num_sms, s);
-  return launch_topo_t<kFP32C, false>(p, dummy, p.n_lines, num_sms, s);
+  const int slots = tuned_topo_slots(prec, p.max_resident_pad > 0, p.n_lines);
+  if (prec == kFP64) return launch_topo_s<kFP64, false>(p, dummy, p.n_lines, num_sms, s, slots);
+  if (p.max_resident_pad > 0)
+    return launch_topo_s<kFP32C, true>(p, dummy, p.n_lines, num_sms, s, slots);
+  return launch_topo_s<kFP32C, false>(p, dummy, p.n_lines, num_sms, s, slots);
 }
 
 }  // namespace cpetgb

@@ -62,3 +62,22 @@ def test_argument_validation_before_device(built):
     L = _lib.lib()
     assert L.cpetgb_field_grid(3, 0, 1, 1, None, None, None, 1, None, None) == _lib.EINVAL
     assert L.cpetgb_topo_hist2d(0, 1, None, 0, 20, None, None, None, None) == _lib.EINVAL
+
+
+def test_tuning_table_round_trip(built):
+    """The autotuner table is host state: keys, bounds and removal."""
+    from pycpet_gb300 import _lib
+
+    L = _lib.lib()
+    assert L.cpetgb_tune_variants(0) == 6 and L.cpetgb_tune_variants(1) == 2
+    k_small = L.cpetgb_tune_key(0, 1, 0, 1e5)
+    k_big = L.cpetgb_tune_key(0, 1, 0, 1e10)
+    assert k_small >= 0 and k_big > k_small
+    assert L.cpetgb_tune_get(k_big) == -1
+    assert L.cpetgb_tune_set(k_big, 4) == 0 and L.cpetgb_tune_get(k_big) == 4
+    assert L.cpetgb_tune_set(k_big, 9) == _lib.EINVAL       # no such variant
+    assert L.cpetgb_tune_set(k_big, -1) == 0 and L.cpetgb_tune_get(k_big) == -1
+    kt = L.cpetgb_tune_key(1, 1, 1, 1e5)
+    assert L.cpetgb_tune_set(kt, 2) == _lib.EINVAL and L.cpetgb_tune_set(kt, 1) == 0
+    assert L.cpetgb_tune_set(kt, -1) == 0
+    assert L.cpetgb_tune_key(7, 1, 0, 1.0) == _lib.EINVAL

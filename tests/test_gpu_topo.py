@@ -142,3 +142,64 @@ def test_batch_of_frames_equals_single_frames(gpu_lib):
                                     precision=prec, return_steps=True)
             np.testing.assert_array_equal(s, ss)
             np.testing.assert_array_equal(r, single)
+
+
+def test_graph_plans_replay(gpu_lib):
+    """CUDA-graph plans (grid and streamline batches) give the direct results,
+    and a replay after the inputs change in place gives the new results."""
+    import torch
+    from pycpet_gb300 import GridBatch, TopoBatch, synchronize
+
+    frames = []
+    for i, (n, L) in enumerate([(1500, 200), (4000, 50), (600, 300)]):
+        x, q, starts, caps, dims, step = _case(n, L, 200 + i)
+        frames.append({"x": x, "q": q, "starts": starts, "n_iter": caps, "step": step, "half_dims": dims})
+    for prec in ("fp32c", "fp64"):
+        direct = TopoBatch(frames, precision=prec, device=True).run()
+        tb = TopoBatch(frames, precision=prec, device=True, graph=True)
+        r1 = tb.run().clone()
+        synchronize()
+        np.testing.assert_array_equal(r1.cpu().numpy(), direct.cpu().numpy())
+        tb.q.mul_(-1.0)                       # reversed charges: new field lines, replay the same graph
+        r2 = tb.run()
+        synchronize()
+        flipped = [dict(fr, q=-fr["q"]) for fr in frames]
+        np.testing.assert_array_equal(r2.cpu().numpy(), TopoBatch(flipped, precision=prec).run())
+    gframes = [(np.random.default_rng(i).uniform(-1, 1, (n, 3)), fr["x"], fr["q"])
+               for i, (n, fr) in enumerate(zip([700, 1331, 64], frames))]
+    for kind in ("field", "esp"):
+        direct = GridBatch(gframes, kind=kind, device=True).run().clone()
+        gb = GridBatch(gframes, kind=kind, device=True, graph=True)
+        out = gb.run()
+        synchronize()
+        np.testing.assert_array_equal(out.cpu().numpy(), direct.cpu().numpy())
+        gb.points.add_(0.25)
+        out = gb.run()
+        synchronize()
+        moved = [(p + 0.25, x, q) for p, x, q in gframes]
+        np.testing.assert_array_equal(out.cpu().numpy(), GridBatch(moved, kind=kind).run())
+
+
+def test_tuned_variants_agree(gpu_lib, oracle):
+    """Every tile-shape variant the autotuner may pick gives parity results:
+    streamline slot counts are bit-identical, grid shapes stay within the
+    FP32C tolerance of the FP64 oracle."""
+    from pycpet_gb300 import _lib, autotune, field_grid, topo_lines
+
+    x, q, starts, caps, dims, step = _case(3000, 600, 300)
+    k = autotune.key(autotune.OP_TOPO, "fp32c", 1, len(starts))
+    out = []
+    for v in range(2):
+        autotune.set_variant(k, v)
+        out.append(topo_lines(starts, caps, x, q, step, dims, precision="fp32c"))
+    autotune.set_variant(k, -1)
+    np.testing.assert_array_equal(out[0], out[1])
+    pts = np.random.default_rng(1).uniform(-1, 1, (3000, 3))
+    ref = oracle.field_grid_f64(pts, x, q)
+    k = autotune.key(autotune.OP_GRID, "fp32c", _lib.FIELD, len(pts) * len(q))
+    for v in range(6):
+        autotune.set_variant(k, v)
+        E = field_grid(pts, x, q, precision="fp32c")
+        err = np.linalg.norm(E - ref, axis=1) / np.linalg.norm(ref, axis=1)
+        assert err.max() <= 1e-5, (v, err.max())
+    autotune.set_variant(k, -1)
