@@ -40,6 +40,7 @@ extern "C" {
 #define CPETGB_ETIMEOUT (-4) /* a bounded device-side wait gave up */
 #define CPETGB_ENODEV (-5)   /* no usable CUDA device */
 #define CPETGB_ERANGE (-6)   /* non-finite or inverted histogram range */
+#define CPETGB_EAGAIN (-7)   /* engine capacity in use: retry after collecting requests */
 
 #define CPETGB_FP64 0
 #define CPETGB_FP32C 1
@@ -155,6 +156,29 @@ int cpetgb_topo_plan_create(cpetgb_plan** plan, int precision, int n_frames, con
                             int32_t* steps);
 int cpetgb_plan_launch(cpetgb_plan* plan, void* stream);
 int cpetgb_plan_destroy(cpetgb_plan* plan);
+
+/* ---- streamline serving engine (continuous batching) --------------------- */
+/* Frames stay resident in a device pool; each submitted request's lines are
+ * published as chunks that a persistent kernel's warps claim while it runs, so
+ * requests arriving while others are in flight are admitted as line slots free
+ * up and their work overlaps on the device.  Results are the same as
+ * cpetgb_topo_lines on the same inputs.  Capacities are fixed at creation; a
+ * request that does not fit gets CPETGB_EAGAIN (admission control).  All data
+ * pointers are HOST pointers.  One thread at a time per engine. */
+typedef struct cpetgb_engine cpetgb_engine;
+int cpetgb_engine_create(cpetgb_engine** engine, int precision, int64_t charge_capacity,
+                         int64_t line_capacity, int max_frames, int max_requests,
+                         int chunk_lines);
+int cpetgb_engine_destroy(cpetgb_engine* engine);
+int cpetgb_engine_add_frame(cpetgb_engine* engine, int n_charges, const double* x, const double* q,
+                            int* frame_id);
+int cpetgb_engine_remove_frame(cpetgb_engine* engine, int frame_id);
+int cpetgb_engine_submit(cpetgb_engine* engine, int frame_id, int n_lines, const double* starts,
+                         const int32_t* n_iter, double step, const double* half_dims,
+                         int* request_id);
+int cpetgb_engine_poll(cpetgb_engine* engine, int request_id);  /* 1 done, 0 pending */
+int cpetgb_engine_collect(cpetgb_engine* engine, int request_id, double* result, int32_t* steps);
+int cpetgb_engine_drain(cpetgb_engine* engine);
 
 /* Streamlines for callers that must not have device memory allocated on their
  * behalf (device memory reserved up front by their own allocator, or a fixed

@@ -12,13 +12,13 @@ import os
 from .build import LIB
 
 OK = 0
-EINVAL, ENOMEM, ECUDA, ETIMEOUT, ENODEV, ERANGE = -1, -2, -3, -4, -5, -6
+EINVAL, ENOMEM, ECUDA, ETIMEOUT, ENODEV, ERANGE, EAGAIN = -1, -2, -3, -4, -5, -6, -7
 FP64, FP32C = 0, 1
 HOST, DEVICE = 0, 1
 FIELD, ESP = 0, 1
 
 _CODES = {EINVAL: "EINVAL", ENOMEM: "ENOMEM", ECUDA: "ECUDA", ETIMEOUT: "ETIMEOUT",
-          ENODEV: "ENODEV", ERANGE: "ERANGE"}
+          ENODEV: "ENODEV", ERANGE: "ERANGE", EAGAIN: "EAGAIN"}
 
 _lib = None
 _path = None
@@ -57,6 +57,14 @@ SIGNATURES = {
     "cpetgb_topo_plan_create": [_vp, _i, _i, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp],
     "cpetgb_plan_launch": [_vp, _vp],
     "cpetgb_plan_destroy": [_vp],
+    "cpetgb_engine_create": [_vp, _i, ctypes.c_int64, ctypes.c_int64, _i, _i, _i],
+    "cpetgb_engine_destroy": [_vp],
+    "cpetgb_engine_add_frame": [_vp, _i, _vp, _vp, _vp],
+    "cpetgb_engine_remove_frame": [_vp, _i],
+    "cpetgb_engine_submit": [_vp, _i, _i, _vp, _vp, _d, _vp, _vp],
+    "cpetgb_engine_poll": [_vp, _i],
+    "cpetgb_engine_collect": [_vp, _i, _vp, _vp],
+    "cpetgb_engine_drain": [_vp],
     "cpetgb_topo_lines_noalloc": [_i, _i, _i, _vp, _vp, _d, _vp, _vp, _vp, _vp, _vp, _vp, _vp],
     "cpetgb_topo_hist2d": [_i, _i, _vp, _i, _i, _vp, _vp, _vp, _vp],
 }

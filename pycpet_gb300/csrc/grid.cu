@@ -320,6 +320,13 @@ template <int PREC, int KIND, int PPT>
 cudaError_t launch_grid_t(int clamp, int n_items, const GridItem* items, const void* packed,
                           const double* points, double* out, double* partial, int* status,
                           cudaStream_t s) {
+  // same carveout as the streamline engine, so both fit on one SM
+  cudaFuncSetAttribute(grid_kernel<PREC, KIND, true, PPT>,
+                       cudaFuncAttributePreferredSharedMemoryCarveout,
+                       cudaSharedmemCarveoutMaxShared);
+  cudaFuncSetAttribute(grid_kernel<PREC, KIND, false, PPT>,
+                       cudaFuncAttributePreferredSharedMemoryCarveout,
+                       cudaSharedmemCarveoutMaxShared);
   if (clamp)
     grid_kernel<PREC, KIND, true, PPT>
         <<<n_items, kGridThreads, 0, s>>>(items, packed, points, out, partial, status);

@@ -117,6 +117,31 @@ cudaError_t launch_pack_topo(int prec, int64_t n, int64_t n_pad, const double* x
 // api.cu: records `msg` as the calling thread's last error and returns `code`.
 int set_error(int code, const char* msg);
 
+// Streamline serving engine (topo.cu kernel, engine.cu host side).
+// A chunk of lines of one request; written by the host into host-mapped memory.
+struct EngineChunk {
+  int32_t frame;       // engine frame slot (index into the frame table)
+  int32_t request;     // request slot (index into the done counters)
+  int32_t line_begin;  // global line indices [line_begin, line_end)
+  int32_t line_end;
+  double step;
+  double half[3];
+};
+static_assert(sizeof(EngineChunk) == 48, "EngineChunk layout");
+
+struct EngineParams {
+  TopoParams p;                 // line arrays (starts, n_iter, result, ends, steps) and status
+  const TopoFrame* frames;      // frame table (packed_off, n_pad) in device memory
+  const EngineChunk* chunks;    // chunk ring (host-mapped)
+  int chunk_capacity;
+  const int* tail;              // chunks published (host-mapped, written by the host)
+  int* head;                    // chunks claimed (device memory)
+  int* head_mirror;             // claims seen by the host (host-mapped, monotonic)
+  int* done;                    // finished lines per request slot (host-mapped)
+};
+cudaError_t launch_engine(int prec, const EngineParams& e, int ctas, cudaStream_t s);
+int engine_threads();
+
 // api.cu: the tuned variants (autotuner table, defaults when untuned).
 int tuned_topo_slots(int prec, bool resident, int n_lines);    // 2 or 4 line slots per warp
 void tuned_grid_shape(int prec, int kind, double pair_evals, int* ppt, int* items_per_sm);

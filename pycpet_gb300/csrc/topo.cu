@@ -497,6 +497,268 @@ __global__ void __launch_bounds__(kTopoThreads, 1) topo_kernel(TopoParams p, Top
   }
 }
 
+// ---------------------------------------------------------------------------
+// Serving engine: continuous batching of streamline requests.
+// ---------------------------------------------------------------------------
+// Warps claim chunks of lines from a ring the host appends to while the
+// kernel runs; a slot that finishes a line takes the next line of the warp's
+// chunk (or of a newly claimed chunk, possibly of another frame), so requests
+// arriving while others are in flight are admitted as slots free up.  Each
+// step the warp sweeps the charges once per distinct frame among its active
+// slots.  Charges are read from global memory (L2).  Nothing waits: a warp
+// that finds no line and no chunk exits; the host launches a new kernel when
+// it publishes work after the previous one may have ended.
+constexpr int kEngineThreads = 256;
+constexpr int kEngineWarps = kEngineThreads / 32;
+constexpr unsigned long long kEngineIdleNs = 50000000ull;  // 50 ms of polling before a warp exits
+
+__device__ __forceinline__ int ld_acquire_sys(const int* p) {
+  int v;
+  asm volatile("ld.acquire.sys.global.s32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+
+// Claims the next published chunk; -1 when none is published.  The claim
+// counter lives in device memory (L2 atomics); every failed CAS means another
+// warp advanced it, so the loop ends within the number of published chunks.
+// The host sees claims through a monotonic mirror in host-mapped memory.
+__device__ int engine_claim(const EngineParams& E) {
+  for (int tries = 0; tries < (1 << 20); ++tries) {
+    const int t = ld_acquire_sys(E.tail);
+    const int h = *reinterpret_cast<volatile int*>(E.head);
+    if (h >= t) return -1;
+    if (atomicCAS(E.head, h, h + 1) == h) {
+      atomicMax_system(E.head_mirror, h + 1);
+      return h;
+    }
+  }
+  return -1;
+}
+
+__device__ __forceinline__ EngineChunk engine_read_chunk(const EngineParams& E, int idx) {
+  const volatile EngineChunk* c = E.chunks + (idx % E.chunk_capacity);
+  EngineChunk r;
+  r.frame = c->frame;
+  r.request = c->request;
+  r.line_begin = c->line_begin;
+  r.line_end = c->line_end;
+  r.step = c->step;
+  r.half[0] = c->half[0];
+  r.half[1] = c->half[1];
+  r.half[2] = c->half[2];
+  return r;
+}
+
+// slot_load for lines the host wrote while the kernel may run: read past L1.
+__device__ void engine_slot_load(Slot& sl, SlotRec& rec, int line, const TopoParams& p) {
+  sl.line = line;
+  const double* s = p.starts + 3 * static_cast<int64_t>(line);
+  double st[3];
+  for (int k = 0; k < 3; ++k) rec.x0[k] = st[k] = __ldcg(s + k);
+  set_pos(sl, st);
+  sl.cap = max(__ldcg(p.n_iter + line), 0);
+  if (sl.cap > kMaxLineCap) {
+    atomicCAS(p.status, kDevOk, kDevBadCap);
+    sl.cap = 0;
+  }
+  sl.steps = 0;
+  if (sl.cap > 0) {
+    sl.phase = kMain;
+  } else {
+    sl.phase = kStart1;
+    for (int k = 0; k < 3; ++k) rec.xend[k] = st[k];
+  }
+}
+
+// Per-slot request context, kept in shared memory (read once per step).
+struct EngineSlotCtx {
+  long long off;  // the frame's first packed element
+  int frame;
+  int req;
+  int n_pad;
+  int pad_;
+  double step;
+  double half[3];
+};
+
+template <int PREC, int S>
+__global__ void __launch_bounds__(kEngineThreads, 2) engine_kernel(EngineParams E) {
+  __shared__ SlotRec recs[kEngineWarps][S];
+  __shared__ EngineSlotCtx sctx[kEngineWarps][S];
+  __shared__ EngineChunk wchunk[kEngineWarps];
+  const int lane = threadIdx.x & 31;
+  const int warp = threadIdx.x >> 5;
+  SlotRec& rec = recs[warp][lane < S ? lane : 0];
+  EngineSlotCtx& my = sctx[warp][lane < S ? lane : 0];
+  const size_t elem = (PREC == kFP32C) ? 16 : 32;
+  if (lane < S) my.frame = -1;
+
+  Slot sl;
+  sl.line = -1;
+  sl.phase = kMain;
+  sl.steps = sl.cap = 0;
+  sl.pos[0] = sl.pos[1] = sl.pos[2] = 0.0;
+  sl.posf[0] = sl.posf[1] = sl.posf[2] = 0.f;
+  int c_next = 0, c_end = 0;  // the warp's chunk cursor (uniform across the warp)
+  int backoff = 0;            // steps to wait before claiming again after an empty queue
+  __syncwarp();
+
+  for (;;) {
+    // refill idle slots, claiming chunks as needed
+    unsigned need = __ballot_sync(0xffffffffu, lane < S && sl.line < 0);
+    const bool all_idle = __popc(need) == S;
+    if (backoff > 0 && !all_idle) {
+      --backoff;
+      need = (c_next < c_end) ? need : 0u;  // only lines of the current chunk
+    }
+    while (need) {
+      if (c_next >= c_end) {
+        int got = -1;
+        if (lane == 0) {
+          got = engine_claim(E);
+          // A warp with nothing to do polls for new chunks for a bounded time
+          // (kEngineIdleNs) before it exits, so the kernel keeps its warps
+          // between arrivals instead of thinning out.
+          if (got < 0 && all_idle) {
+            const unsigned long long t0 = globaltimer_ns();
+            while (got < 0 && globaltimer_ns() - t0 < kEngineIdleNs) {
+              __nanosleep(20000);
+              got = engine_claim(E);
+            }
+          }
+          if (got >= 0) wchunk[warp] = engine_read_chunk(E, got);
+        }
+        got = __shfl_sync(0xffffffffu, got, 0);
+        __syncwarp();
+        if (got < 0) {
+          backoff = 8;
+          break;
+        }
+        c_next = wchunk[warp].line_begin;
+        c_end = wchunk[warp].line_end;
+        continue;
+      }
+      const int target = __ffs(need) - 1;
+      const int line = c_next++;
+      if (lane == target) {
+        const EngineChunk& ch = wchunk[warp];
+        // frame slots are reused while the kernel runs: read the table past L1
+        my.off = __ldcg(&E.frames[ch.frame].packed_off);
+        my.frame = ch.frame;
+        my.req = ch.request;
+        my.n_pad = __ldcg(&E.frames[ch.frame].n_pad);
+        my.step = ch.step;
+        for (int k = 0; k < 3; ++k) my.half[k] = ch.half[k];
+        engine_slot_load(sl, rec, line, E.p);
+      }
+      need &= ~(1u << target);
+      __syncwarp();
+    }
+    const unsigned active = __ballot_sync(0xffffffffu, lane < S && sl.line >= 0);
+    if (active == 0) break;
+
+    double nx[3] = {0.0, 0.0, 0.0};
+    unsigned remaining = active;
+    while (remaining) {
+      const int leader = __ffs(remaining) - 1;
+      const EngineSlotCtx& L = sctx[warp][leader];
+      const int f = L.frame;
+      const unsigned group =
+          __ballot_sync(0xffffffffu, lane < S && sl.line >= 0 && my.frame == f) & remaining;
+      remaining &= ~group;
+      const int na = __popc(group);
+      const int n_pad = L.n_pad;
+      const ulonglong2* gA = reinterpret_cast<const ulonglong2*>(
+          static_cast<const char*>(E.p.packed) + L.off * static_cast<long long>(elem));
+      const ulonglong2* gB = gA + n_pad / 2;
+      int src_of[S];
+      int my_rank = -1;
+      {
+        unsigned m = group;
+#pragma unroll
+        for (int e = 0; e < S; ++e) {
+          src_of[e] = m ? (__ffs(m) - 1) : 0;
+          if (m) m &= m - 1;
+          if (src_of[e] == lane && e < na) my_rank = e;
+        }
+      }
+      if constexpr (PREC == kFP32C) {
+        uint64_t ex2[S][3];
+#pragma unroll
+        for (int e = 0; e < S; ++e)
+#pragma unroll
+          for (int c = 0; c < 3; ++c) {
+            const float v = __shfl_sync(0xffffffffu, sl.posf[c], src_of[e]);
+            ex2[e][c] = pk2(v, v);
+          }
+        float total;
+        const int n_pairs = n_pad / 2;
+        switch (na) {
+          case 1: sweep_f32x2<1, S>(gA, gB, n_pairs, lane, ex2, total); break;
+          case 2: sweep_f32x2<2, S>(gA, gB, n_pairs, lane, ex2, total); break;
+          case 3: sweep_f32x2<(S > 2 ? 3 : 2), S>(gA, gB, n_pairs, lane, ex2, total); break;
+          default: sweep_f32x2<S, S>(gA, gB, n_pairs, lane, ex2, total); break;
+        }
+        float Ef[3];
+        const int rk = my_rank >= 0 ? my_rank : 0;
+#pragma unroll
+        for (int c = 0; c < 3; ++c)
+          Ef[c] = __shfl_sync(0xffffffffu, total, (3 * rk + c) << (S == 4 ? 1 : 2));
+        if (my_rank >= 0) {
+          const float n2 =
+              __fmaf_rn(Ef[0], Ef[0], __fmaf_rn(Ef[1], Ef[1], __fmul_rn(Ef[2], Ef[2])));
+          const float st = __fdiv_rn(static_cast<float>(my.step), __fsqrt_rn(n2));
+#pragma unroll
+          for (int c = 0; c < 3; ++c) nx[c] = sl.pos[c] + static_cast<double>(__fmul_rn(Ef[c], st));
+        }
+      } else {
+        double ex[S][3];
+#pragma unroll
+        for (int e = 0; e < S; ++e)
+#pragma unroll
+          for (int c = 0; c < 3; ++c) ex[e][c] = __shfl_sync(0xffffffffu, sl.pos[c], src_of[e]);
+        double Es[S][3];
+        const Charge64* g = reinterpret_cast<const Charge64*>(gA);
+        switch (na) {
+          case 1: sweep_f64<1, S>(g, n_pad, lane, ex, Es); break;
+          case 2: sweep_f64<2, S>(g, n_pad, lane, ex, Es); break;
+          case 3: sweep_f64<(S > 2 ? 3 : 2), S>(g, n_pad, lane, ex, Es); break;
+          default: sweep_f64<S, S>(g, n_pad, lane, ex, Es); break;
+        }
+        if (my_rank >= 0) {
+          double Ev[3] = {0.0, 0.0, 0.0};
+#pragma unroll
+          for (int e = 0; e < S; ++e)
+            if (e == my_rank)
+#pragma unroll
+              for (int c = 0; c < 3; ++c) Ev[c] = Es[e][c];
+          const double n = sqrt(Ev[0] * Ev[0] + Ev[1] * Ev[1] + Ev[2] * Ev[2]);
+#pragma unroll
+          for (int c = 0; c < 3; ++c) nx[c] = sl.pos[c] + my.step * Ev[c] / n;
+        }
+      }
+    }
+
+    if (lane < S && sl.line >= 0) {
+      FrameCtx fc;
+      fc.line_off = 0;
+      fc.n_lines = 0;
+      fc.step = my.step;
+#pragma unroll
+      for (int k = 0; k < 3; ++k) {
+        fc.half[k] = my.half[k];
+        fc.hf[k] = static_cast<float>(my.half[k]);
+      }
+      if (slot_advance<PREC == kFP32C>(sl, rec, nx, E.p, fc)) {
+        __threadfence_system();  // the line's results before its completion count
+        atomicAdd_system(E.done + my.req, 1);
+        sl.line = -1;
+      }
+    }
+    __syncwarp();
+  }
+}
+
 __global__ void pack_pairs_kernel(int64_t n, int64_t n_pad, const double* __restrict__ x,
                                   const double* __restrict__ q, float4* __restrict__ out) {
   const int64_t n_pairs = n_pad / 2;
@@ -596,6 +858,28 @@ __global__ void pack_frames_kernel(int prec, const TopoFrame* __restrict__ frame
 }  // namespace
 
 int topo_charge_pad(int prec) { return prec == kFP32C ? kChargePad32 : kChargePad64; }
+
+int engine_threads() { return kEngineThreads; }
+
+// The engine runs beside grid launches: its SMs keep the largest shared-memory
+// carveout so grid blocks (33 KB of staged charge tiles) fit next to it.
+cudaError_t launch_engine(int prec, const EngineParams& e, int ctas, cudaStream_t s) {
+  cudaError_t err;
+  if (prec == kFP32C) {
+    err = cudaFuncSetAttribute(engine_kernel<kFP32C, 4>,
+                               cudaFuncAttributePreferredSharedMemoryCarveout,
+                               cudaSharedmemCarveoutMaxShared);
+    if (err != cudaSuccess) return err;
+    engine_kernel<kFP32C, 4><<<ctas, kEngineThreads, 0, s>>>(e);
+  } else {
+    err = cudaFuncSetAttribute(engine_kernel<kFP64, 4>,
+                               cudaFuncAttributePreferredSharedMemoryCarveout,
+                               cudaSharedmemCarveoutMaxShared);
+    if (err != cudaSuccess) return err;
+    engine_kernel<kFP64, 4><<<ctas, kEngineThreads, 0, s>>>(e);
+  }
+  return cudaGetLastError();
+}
 
 size_t topo_resident_limit(int prec) {
   if (prec != kFP32C) return 0;  // FP64 charges are read from global memory (L2)
