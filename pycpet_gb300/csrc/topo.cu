@@ -45,8 +45,8 @@ namespace {
 
 constexpr int kTopoThreads = 512;
 constexpr int kTopoWarps = kTopoThreads / 32;
-constexpr int kLanePairs = 16;                  // charge pairs per lane between Kahan steps
-constexpr int kChargePad32 = 32 * kLanePairs * 2;  // FP32C frames: multiple of 1024 charges
+constexpr int kLanePairs = 32;                  // charge pairs per lane between Kahan steps
+constexpr int kChargePad32 = 64;                // FP32C frames: one charge pair per lane
 constexpr int kChargePad64 = 256;               // FP64 frames
 // Line slots per warp S (template parameter): 4 (default) or 2.
 
@@ -201,7 +201,31 @@ __device__ bool slot_advance(Slot& sl, SlotRec& rec, const double nx[3], const T
 // B[p] = {z_2p, z_2p+1, q_2p, q_2p+1}, so each 64-bit half of a 16-byte load is
 // a ready operand of the packed f32x2 instructions: one instruction evaluates
 // a pair term for two charges.  Lanes take pairs lane-strided; every
-// kLanePairs pairs the two packed streams are added and Kahan-accumulated.
+// kLanePairs pairs (fewer in a frame's last run: frames are padded to one pair
+// per lane only) the two packed streams are added and Kahan-accumulated.
+template <int NA, int S, int UNROLL>
+__device__ __forceinline__ void pair_run(const ulonglong2* __restrict__ A,
+                                         const ulonglong2* __restrict__ B, int base, int cnt,
+                                         const uint64_t (&ex2)[S][3], uint64_t (&part)[NA][3]) {
+#pragma unroll UNROLL
+  for (int i = 0; i < cnt; ++i) {
+    const ulonglong2 a = A[base + 32 * i];  // {x pair, y pair}
+    const ulonglong2 b = B[base + 32 * i];  // {z pair, q pair}
+#pragma unroll
+    for (int e = 0; e < NA; ++e) {
+      const uint64_t dx = sub2(ex2[e][0], a.x);
+      const uint64_t dy = sub2(ex2[e][1], a.y);
+      const uint64_t dz = sub2(ex2[e][2], b.x);
+      const uint64_t r2 = fma2(dx, dx, fma2(dy, dy, mul2(dz, dz)));
+      const uint64_t ri = rsqrt2(r2);
+      const uint64_t w = mul2(mul2(b.y, ri), mul2(ri, ri));
+      part[e][0] = fma2(w, dx, part[e][0]);
+      part[e][1] = fma2(w, dy, part[e][1]);
+      part[e][2] = fma2(w, dz, part[e][2]);
+    }
+  }
+}
+
 template <int NA, int S>
 __device__ __forceinline__ void sweep_f32x2(const ulonglong2* __restrict__ A,
                                             const ulonglong2* __restrict__ B, int n_pairs,
@@ -213,29 +237,20 @@ __device__ __forceinline__ void sweep_f32x2(const ulonglong2* __restrict__ A,
 #pragma unroll
     for (int c = 0; c < 3; ++c) acc[e][c] = cmp[e][c] = 0.f;
 
-  for (int base = lane; base < n_pairs; base += 32 * kLanePairs) {
+  // n_pairs is a multiple of 32: every lane runs the same number of pairs
+  for (int base = 0; base < n_pairs; base += 32 * kLanePairs) {
     uint64_t part[NA][3];
 #pragma unroll
     for (int e = 0; e < NA; ++e)
 #pragma unroll
       for (int c = 0; c < 3; ++c) part[e][c] = 0ull;
-#pragma unroll 4
-    for (int i = 0; i < kLanePairs; ++i) {
-      const ulonglong2 a = A[base + 32 * i];  // {x pair, y pair}
-      const ulonglong2 b = B[base + 32 * i];  // {z pair, q pair}
-#pragma unroll
-      for (int e = 0; e < NA; ++e) {
-        const uint64_t dx = sub2(ex2[e][0], a.x);
-        const uint64_t dy = sub2(ex2[e][1], a.y);
-        const uint64_t dz = sub2(ex2[e][2], b.x);
-        const uint64_t r2 = fma2(dx, dx, fma2(dy, dy, mul2(dz, dz)));
-        const uint64_t ri = rsqrt2(r2);
-        const uint64_t w = mul2(mul2(b.y, ri), mul2(ri, ri));
-        part[e][0] = fma2(w, dx, part[e][0]);
-        part[e][1] = fma2(w, dy, part[e][1]);
-        part[e][2] = fma2(w, dz, part[e][2]);
-      }
-    }
+    const int left = (n_pairs - base) >> 5;
+    // about eight independent pair chains in flight per lane: unroll 8 / NA
+    constexpr int kUnroll = NA >= 3 ? 2 : (NA == 2 ? 4 : 8);
+    if (left >= kLanePairs)
+      pair_run<NA, S, kUnroll>(A, B, base + lane, kLanePairs, ex2, part);
+    else
+      pair_run<NA, S, 1>(A, B, base + lane, left, ex2, part);
 #pragma unroll
     for (int e = 0; e < NA; ++e)
 #pragma unroll
