@@ -247,6 +247,7 @@ def main():
     for _ in range(args.warmup):
         step()
     ffma = _lib.measure_peak(0)  # FP32 pipe peak of this GPU, measured now
+    loop_rate = _lib.measure_peak(4)  # the sweep's inner loop alone (pair evaluations/s)
     torch.cuda.synchronize()
 
     evs = [[torch.cuda.Event(enable_timing=True) for _ in range(4)] for _ in range(args.steps)]
@@ -298,10 +299,12 @@ def main():
                      "traffic_note": "DRAM bytes per launch (ncu capture of 20,000 lines scaled by lines); "
                                      "the kernel is FP32-pipe bound, the charges stay in shared memory",
                      "frac_ceiling": 17 / 24,
+                     "sweep_loop_pair_evals_per_s": loop_rate,
+                     "frac_of_sweep_loop": (pe_step / avg_kern_s) / loop_rate,
                      "kernel": "topo_kernel (FP32C, charges resident in shared memory)",
                      "work": f"{FLOPS_PER_PAIR} flop per pair evaluation x sum_lines N*(max(s,2)+2)",
                      "peak_source": "FFMA throughput measured in this run (cpetgb_measure_peak); "
-                                    "the driver's peak file has no FP32 figure"},
+                                    "MEASURED_PEAKS.json holds HBM and bf16 figures only"},
         "gpu_launches": 4 * args.steps,
         "clocks": clocks,
     }

@@ -64,7 +64,8 @@ int cpetgb_set_default_precision(int precision);
 int cpetgb_get_default_precision(void);
 
 /* Pipe throughput microbenchmark on the current device (roofline denominators):
- * kind 0 FP32 FFMA flop/s, 1 FP64 DFMA flop/s, 2 MUFU rsqrt op/s, 3 FP32x2 FFMA2 flop/s. */
+ * kind 0 FP32 FFMA flop/s, 1 FP64 DFMA flop/s, 2 MUFU rsqrt op/s, 3 FP32x2 FFMA2 flop/s,
+ * 4 pair evaluations/s of the FP32C streamline sweep's inner loop alone. */
 int cpetgb_measure_peak(int kind, double* ops_per_s);
 
 /* ---- float32 drop-ins of the reference FFI (host buffers) ---------------- */
@@ -128,14 +129,19 @@ int cpetgb_topo_batch(int precision, int mem, int n_frames, const int64_t* desc,
 /* ---- autotuner table ------------------------------------------------------ */
 /* Tile shapes are chosen per (operation, precision, class, size bucket):
  *   op 0 = grid sums: class = CPETGB_FIELD / CPETGB_ESP, size = pair evaluations
- *          of the launch (buckets of x4 from 1e6); variants 0..5 = points per
- *          thread {4, 8} x work items per SM {4, 8, 16} (default 1);
+ *          of the launch (buckets of x4 from 1e6); variants 0..9 = points per
+ *          thread {4, 8} x work items per SM {4, 8, 16, 32, 64} (default 1);
  *   op 1 = streamlines: class = 1 if the frame's charges stay in shared memory,
  *          size = lines (buckets of x4 from 1e3); variants 0..1 = line slots per
  *          warp {4, 2} (default 0).
+ * A launch whose own bucket is untuned uses the nearest tuned bucket of the
+ * same (operation, precision, class), else the default.
  * pycpet_gb300.autotune times the candidates and fills the table. */
 int cpetgb_tune_key(int op, int precision, int cls, double size);
 int cpetgb_tune_variants(int op);
+/* Largest frame (charges) whose streamline charges are held in shared memory
+ * for the whole launch on the current device (the tuner's class 1); 0 for FP64. */
+int cpetgb_topo_resident_limit(int precision);
 int cpetgb_tune_set(int key, int variant);   /* variant -1 removes the entry */
 int cpetgb_tune_get(int key);                /* -1 when untuned */
 

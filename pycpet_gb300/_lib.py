@@ -53,6 +53,7 @@ SIGNATURES = {
     "cpetgb_tune_variants": [_i],
     "cpetgb_tune_set": [_i, _i],
     "cpetgb_tune_get": [_i],
+    "cpetgb_topo_resident_limit": [_i],
     "cpetgb_grid_plan_create": [_vp, _i, _i, _i, _i, _vp, _vp, _vp, _vp, _vp],
     "cpetgb_topo_plan_create": [_vp, _i, _i, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp],
     "cpetgb_plan_launch": [_vp, _vp],
@@ -121,7 +122,8 @@ def check(rc: int) -> None:
 
 
 def measure_peak(kind: int) -> float:
-    """Measured pipe throughput (0 FFMA flop/s, 1 DFMA flop/s, 2 MUFU op/s, 3 FFMA2 flop/s)."""
+    """Measured throughput: 0 FFMA flop/s, 1 DFMA flop/s, 2 MUFU op/s, 3 FFMA2 flop/s,
+    4 pair evaluations/s of the FP32C streamline sweep's inner loop alone."""
     v = ctypes.c_double(0.0)
     check(lib().cpetgb_measure_peak(kind, ctypes.byref(v)))
     return v.value

@@ -3,7 +3,7 @@
 The library picks a kernel variant per (operation, precision, class, size
 bucket) from a table (see ``cpetgb_tune_*`` in include/cpetgb.h):
 
-* grid sums (op 0): points per thread {4, 8} x work items per SM {4, 8, 16};
+* grid sums (op 0): points per thread {4, 8} x work items per SM {4, 8, 16, 32, 64};
   class = field / potential; size = pair evaluations of the launch;
 * streamlines (op 1): line slots per warp {4, 2}; class = charges resident
   in shared memory or streamed from L2; size = number of lines.
@@ -129,9 +129,11 @@ def tune_topo(frames, precision="fp32c", reps=2, verbose=False):
     tb = TopoBatch(frames, precision=precision, device=True)
     from ._lib import FP32C
 
-    resident_limit = 13312  # charges that fit the shared-memory copy (FP32C)
+    resident_limit = lib().cpetgb_topo_resident_limit(precision_code(precision))
+    check(min(resident_limit, 0))
+    pad = 64  # FP32C streamline frames are padded to a multiple of 64 charges
     n_max = max(len(np.asarray(fr["q"]).reshape(-1)) for fr in frames)
-    cls = 1 if (precision_code(precision) == FP32C and n_max <= resident_limit) else 0
+    cls = 1 if (precision_code(precision) == FP32C and -(-n_max // pad) * pad <= resident_limit) else 0
     k = key(OP_TOPO, precision, cls, tb.n_lines)
     n_var = lib().cpetgb_tune_variants(OP_TOPO)
     times = []
@@ -172,6 +174,9 @@ def tune_default(verbose=True, quick=False):
         [(int(n), h, None) for n, h in zip(np.linspace(3000, 40000, 16 if quick else 64),
                                            [0.5, 1.0, 1.5] * 22)],  # frame batch
     ]
+    rng = np.random.default_rng(2024)  # 48 frames of random sizes: the size bucket below
+    grid_cases.append([(int(n), float(h), None) for n, h in zip(rng.integers(3000, 40001, 48),
+                                                                rng.choice([0.5, 1.0, 1.5], 48))])
     for case in grid_cases:
         frames = grid_frames(case)
         for kind in ("field", "esp"):

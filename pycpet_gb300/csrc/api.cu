@@ -169,7 +169,7 @@ std::mutex g_tune_mu;
 std::map<int, int> g_tune;
 
 constexpr int kOpGrid = 0, kOpTopo = 1;
-constexpr int kGridVariants = 6;  // points per thread {4, 8} x work items per SM {4, 8, 16}
+constexpr int kGridVariants = 10;  // points per thread {4, 8} x work items per SM {4, 8, 16, 32, 64}
 constexpr int kTopoVariants = 2;  // line slots per warp {4, 2}
 
 int size_bucket(double v, double base) {
@@ -187,6 +187,24 @@ int tune_lookup(int key) {
   std::lock_guard<std::mutex> lock(g_tune_mu);
   auto it = g_tune.find(key);
   return it == g_tune.end() ? -1 : it->second;
+}
+
+// The variant for a launch: the entry of its own size bucket, else that of the
+// nearest tuned bucket of the same (operation, precision, class), the smaller
+// one on a tie; -1 when nothing of that class is tuned.
+int tune_choose(int key) {
+  std::lock_guard<std::mutex> lock(g_tune_mu);
+  auto it = g_tune.find(key);
+  if (it != g_tune.end()) return it->second;
+  const int b = key & 15;
+  for (int d = 1; d < 16; ++d) {
+    for (int nb : {b - d, b + d}) {
+      if (nb < 0 || nb > 15) continue;
+      auto jt = g_tune.find((key & ~15) | nb);
+      if (jt != g_tune.end()) return jt->second;
+    }
+  }
+  return -1;
 }
 
 void plan_grid(int n_frames, const int64_t* desc, int sms, GridPlan& plan, int ppt,
@@ -740,16 +758,16 @@ int topo_plan_impl(cpetgb_plan** out_plan, int prec, int F, const int64_t* desc,
 int cpetgb::set_error(int code, const char* msg) { return fail(code, "%s", msg); }
 
 int cpetgb::tuned_topo_slots(int prec, bool resident, int n_lines) {
-  const int v = tune_lookup(tune_key(kOpTopo, prec, resident ? 1 : 0, double(n_lines)));
+  const int v = tune_choose(tune_key(kOpTopo, prec, resident ? 1 : 0, double(n_lines)));
   return v == 1 ? 2 : 4;
 }
 
 void cpetgb::tuned_grid_shape(int prec, int kind, double pair_evals, int* ppt, int* items_per_sm) {
-  int v = tune_lookup(tune_key(kOpGrid, prec, kind, pair_evals));
+  int v = tune_choose(tune_key(kOpGrid, prec, kind, pair_evals));
   if (v < 0 || v >= kGridVariants) v = 1;  // untuned: 4 points per thread, 8 items per SM
-  static const int ips[3] = {4, 8, 16};
-  *ppt = (v / 3) == 1 ? 8 : 4;
-  *items_per_sm = ips[v % 3];
+  static const int ips[5] = {4, 8, 16, 32, 64};
+  *ppt = (v / 5) == 1 ? 8 : 4;
+  *items_per_sm = ips[v % 5];
 }
 
 extern "C" {
@@ -844,6 +862,13 @@ int cpetgb_tune_variants(int op) {
   if (op == kOpGrid) return kGridVariants;
   if (op == kOpTopo) return kTopoVariants;
   return fail(CPETGB_EINVAL, "bad operation %d", op);
+}
+
+int cpetgb_topo_resident_limit(int precision) {
+  if (!valid_prec(precision)) return fail(CPETGB_EINVAL, "bad precision %d", precision);
+  int rc;
+  if (!context(&rc)) return rc;
+  return static_cast<int>(topo_resident_limit(precision));
 }
 
 int cpetgb_tune_set(int key, int variant) {

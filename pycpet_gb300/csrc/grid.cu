@@ -74,7 +74,7 @@ __device__ __forceinline__ void kahan_add2(uint64_t& s, uint64_t& c, uint64_t t)
   s = u;
 }
 
-constexpr int kKahanRun = 16;  // FP32C: charges summed plainly between Kahan steps
+constexpr int kKahanRun = 32;  // FP32C: charges summed plainly between Kahan steps
 
 // FP32C body: this thread's points as G packed pairs (points k = 2g, 2g+1).
 template <int KIND, bool CLAMP, int G>
