@@ -208,6 +208,31 @@ int cpetgb_topo_lines_noalloc(int precision, int n_lines, int n_charges, const d
 int cpetgb_topo_hist2d(int mem, int n_lines, const double* result, int nb_dist, int nb_curv,
                        const double* range, uint64_t* counts, double* edges, void* stream);
 
+/* ---- clustering front end: histograms and distance matrices -------------- */
+/* Histograms of many (distance, curvature) sets with one binning, in one
+ * launch; replaces the per-file np.histogram2d loop of make_histograms
+ * (CPET/utils/calculator.py:689-711).  Set f is rows offsets[f] ..
+ * offsets[f+1]-1 of values[L][2]; offsets is a HOST array [n_sets + 1]
+ * (non-decreasing, offsets[0] = 0); range is a HOST {dist_lo, dist_hi,
+ * curv_lo, curv_hi}, finite with lo <= hi (make_histograms passes the global
+ * min / max).  counts [n_sets][nb_dist*nb_curv] (uint64) and hists (double,
+ * each set divided by its total as make_histograms does, NaN for an empty set)
+ * may each be NULL, not both.  nb_dist + nb_curv <= 4096. */
+int cpetgb_topo_hist2d_sets(int mem, int n_sets, const int64_t* offsets, const double* values,
+                            int nb_dist, int nb_curv, const double* range, uint64_t* counts,
+                            double* hists, void* stream);
+/* Chi-square distance matrix of n histograms (rows of hists[n][bins]):
+ * out[i][j] = 1/2 sum_k (a_k - b_k)^2 / (a_k + b_k) over bins with
+ * a_k + b_k != 0, zero diagonal, out [n][n].  Replaces construct_distance_matrix
+ * with the metric distance_numpy (CPET/utils/calculator.py:975-978, 1003-1015). */
+int cpetgb_chi2_distance_matrix(int precision, int mem, int n, int bins, const double* hists,
+                                double* out, void* stream);
+/* Distance matrix of n vector fields on a common grid (fields[n][n_points][3]):
+ * out[i][j] = sum_p |f_i[p] - f_j[p]|, zero diagonal, out [n][n].  Replaces
+ * construct_distance_matrix_volume (CPET/utils/calculator.py:1042-1058). */
+int cpetgb_field_distance_matrix(int precision, int mem, int n, int n_points,
+                                 const double* fields, double* out, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

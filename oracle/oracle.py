@@ -12,6 +12,9 @@ oracle_ref32.c by oracle/Makefile) and exposes numpy-level wrappers:
   the timed CPU baseline ("port").
 * ``histogram2d``: numpy's own histogram2d, the function the reference calls in
   make_histograms (CPET/utils/calculator.py:702-707).
+* ``chi2_matrix_f64`` / ``field_matrix_f64``: the clustering distance matrices
+  construct_distance_matrix (calculator.py:975-978, 1003-1015) and
+  construct_distance_matrix_volume (calculator.py:1042-1058) in IEEE double.
 * ``load_reference()``: the reference's own math_module.c compiled from source
   into oracle/_ref (present only where the reference checkout exists).
 """
@@ -54,6 +57,8 @@ def lib():
             _c_int, _c_int, _i, ctypes.c_double, _d, _d, _d, _d, _d, _d, _i, _c_int]
         L.oracle_topo_lines_f32_mt.argtypes = [
             _c_int, _c_int, _i, ctypes.c_float, _f, _f, _f, _f, _f, _f, _i, _c_int]
+        L.oracle_chi2_matrix_f64.argtypes = [_c_int, _c_int, _d, _d, _c_int]
+        L.oracle_field_matrix_f64.argtypes = [_c_int, _c_int, _d, _d, _c_int]
         _LIB = L
     return _LIB
 
@@ -132,6 +137,28 @@ def histogram2d(dist, curv, bins, rng):
     """The reference's binning call (CPET/utils/calculator.py:702-707): numpy's histogram2d."""
     h, _, _ = np.histogram2d(np.asarray(dist, np.float64), np.asarray(curv, np.float64), bins=bins, range=rng)
     return h
+
+
+def chi2_matrix_f64(hists, threads=None):
+    """construct_distance_matrix / distance_numpy (CPET/utils/calculator.py:975-978,
+    1003-1015) in IEEE double: (F, B) histograms -> (F, F)."""
+    h = _c(hists, np.float64)
+    n = h.shape[0]
+    out = np.empty((n, n))
+    if n:
+        lib().oracle_chi2_matrix_f64(n, h.shape[1], h.reshape(n, -1), out, _threads(threads))
+    return out
+
+
+def field_matrix_f64(fields, threads=None):
+    """construct_distance_matrix_volume (CPET/utils/calculator.py:1042-1058) in
+    IEEE double: (F, P, 3) fields -> (F, F)."""
+    f = _c(fields, np.float64)
+    n = f.shape[0]
+    out = np.empty((n, n))
+    if n:
+        lib().oracle_field_matrix_f64(n, f.shape[1], f.reshape(n, -1), out, _threads(threads))
+    return out
 
 
 def load_reference():

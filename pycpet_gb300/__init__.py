@@ -7,7 +7,7 @@ math functions of ``CPET.utils.calculator`` (``calculator``) and the
 calculator hot-path methods (``drop_in``).
 """
 from ._lib import CpetgbError  # noqa: F401
-from .core import (GridBatch, TopoBatch, esp_grid, field_grid, point_field, synchronize, topo_hist2d,  # noqa: F401
-                   topo_lines)
+from .core import (GridBatch, TopoBatch, chi2_distance_matrix, esp_grid, field_distance_matrix,  # noqa: F401
+                   field_grid, point_field, synchronize, topo_hist2d, topo_hist2d_sets, topo_lines)
 
 __version__ = "1.0.0"

@@ -14,7 +14,12 @@ Math wrappers (GPU):
   calculate_thread_c_shared                  calculator.py:344-348  -> (2,) float32
 Streamline post-processing and histograms:
   curv / compute_curv_and_dist               calculator.py:501-561  (numpy, host)
-  make_histograms                            calculator.py:596-718  (GPU binning)
+  make_histograms                            calculator.py:596-718  (GPU binning, one launch)
+Clustering front end (GPU distance matrices):
+  distance_numpy                             calculator.py:975-978  (numpy, per pair)
+  construct_distance_matrix                  calculator.py:1003-1015
+  make_fields                                calculator.py:846-857  (host parser)
+  construct_distance_matrix_volume           calculator.py:1042-1058
 """
 from __future__ import annotations
 
@@ -23,8 +28,9 @@ import warnings
 
 import numpy as np
 
+from . import _lib
 from .c_ops import Math_ops
-from .core import topo_hist2d
+from .core import chi2_distance_matrix, field_distance_matrix, topo_hist2d_sets
 
 log = logging.getLogger(__name__)
 
@@ -189,8 +195,52 @@ def make_histograms(topo_files, plot=False):
     dist_all = np.concatenate([d for d, _ in data])
     curv_all = np.concatenate([c for _, c in data])
     bins, rng = histogram_bins(dist_all, curv_all, n_ref)
-    hists = []
-    for d, c in data:
-        counts = topo_hist2d(np.column_stack([d, c]), bins=bins, range=rng).astype(np.float64)
-        hists.append((counts / np.sum(counts)).flatten())
-    return np.array(hists)
+    offsets = np.concatenate([[0], np.cumsum(lens)])
+    # every file's histogram in one launch, each divided by its own total
+    return topo_hist2d_sets(np.column_stack([dist_all, curv_all]), offsets, bins, rng, normalize=True)
+
+
+def distance_numpy(hist1, hist2):
+    """Chi-square distance of two histograms (CPET/utils/calculator.py:975-978),
+    numpy on the host: the per-pair metric; whole matrices go to the GPU
+    through construct_distance_matrix."""
+    a = (hist1 - hist2) ** 2
+    b = hist1 + hist2
+    return np.sum(np.divide(a, b, out=np.zeros_like(a), where=b != 0)) / 2.0
+
+
+def construct_distance_matrix(histograms, precision=None):
+    """All-pairs distance_numpy matrix of the rows of `histograms`
+    (CPET/utils/calculator.py:1003-1015), one GPU launch; zero diagonal.
+    precision: "fp64" (IEEE double) or "fp32c" (FP32 terms, compensated sums);
+    default: the library's default precision."""
+    return chi2_distance_matrix(np.asarray(histograms, np.float64), _precision(precision))
+
+
+def make_fields(field_files):
+    """The (Ex, Ey, Ez) columns of volume .dat files, one (P,3) array per file
+    (CPET/utils/calculator.py:846-857)."""
+    fields = []
+    for field_file in field_files:
+        rows = []
+        with open(field_file) as fh:
+            for line in fh:
+                if line.startswith("#"):
+                    continue
+                parts = line.split()
+                rows.append([float(parts[3]), float(parts[4]), float(parts[5])])
+        fields.append(np.array(rows))
+    return fields
+
+
+def construct_distance_matrix_volume(fields, precision=None):
+    """Matrix of sum_p |f_i[p] - f_j[p]| over a common grid
+    (CPET/utils/calculator.py:1042-1058), one GPU launch; zero diagonal."""
+    return field_distance_matrix(np.stack([np.asarray(f, np.float64).reshape(-1, 3) for f in fields]),
+                                 _precision(precision))
+
+
+def _precision(p):
+    if p is not None:
+        return p
+    return "fp64" if _lib.lib().cpetgb_get_default_precision() == _lib.FP64 else "fp32c"

@@ -395,3 +395,76 @@ def topo_hist2d(result, bins=(20, 20), range=((0.0, 5.2), (0.0, None)), return_e
     if return_edges:
         return counts, edges[:nb0 + 1], edges[nb0 + 1:]
     return counts
+
+
+# ---------------------------------------------------------------------------
+# Clustering front end: histogram sets and distance matrices
+# ---------------------------------------------------------------------------
+
+def topo_hist2d_sets(values, offsets, bins, range, normalize=True):
+    """Histograms of many (distance, curvature) sets with one binning, in one
+    launch (the per-file np.histogram2d loop of make_histograms,
+    CPET/utils/calculator.py:689-711).  values (L,2); set f is rows
+    offsets[f]:offsets[f+1].  range ((d_lo, d_hi), (c_lo, c_hi)) finite.
+    Returns (F, nb0*nb1) float64 histograms each divided by its total
+    (normalize=True, make_histograms' output rows) or int64 counts."""
+    nb0, nb1 = (int(bins), int(bins)) if np.isscalar(bins) else (int(bins[0]), int(bins[1]))
+    rng = np.array([float(v) for pair in range for v in pair], dtype=np.float64)
+    off = np.ascontiguousarray(offsets, dtype=np.int64).reshape(-1)
+    n_sets = len(off) - 1
+    if _is_torch(values):
+        import torch
+
+        values = _dev(values, torch.float64, (2,))
+        dev = values.device
+        out = torch.empty((n_sets, nb0 * nb1), dtype=torch.float64 if normalize else torch.int64, device=dev)
+        with torch.cuda.device(dev):
+            check(lib().cpetgb_topo_hist2d_sets(DEVICE, n_sets, off.ctypes.data, values.data_ptr(), nb0, nb1,
+                                                rng.ctypes.data, None if normalize else out.data_ptr(),
+                                                out.data_ptr() if normalize else None, _stream_of(values)))
+        return out
+    values = _host(values, np.float64, (2,))
+    out = np.empty((n_sets, nb0 * nb1), dtype=np.float64 if normalize else np.uint64)
+    check(lib().cpetgb_topo_hist2d_sets(HOST, n_sets, off.ctypes.data, values.ctypes.data, nb0, nb1,
+                                        rng.ctypes.data, None if normalize else out.ctypes.data,
+                                        out.ctypes.data if normalize else None, None))
+    return out if normalize else out.astype(np.int64)
+
+
+def _distance_matrix(fn, rows, tail, precision):
+    prec = precision_code(precision)
+    if _is_torch(rows):
+        import torch
+
+        rows = _dev(rows, torch.float64)
+        n = rows.shape[0]
+        feat = rows[0].numel() // tail if n else 0
+        out = torch.empty((n, n), dtype=torch.float64, device=rows.device)
+        with torch.cuda.device(rows.device):
+            check(fn(prec, DEVICE, n, feat, rows.data_ptr(), out.data_ptr(), _stream_of(rows)))
+        return out
+    rows = np.ascontiguousarray(rows, dtype=np.float64)
+    n = rows.shape[0]
+    feat = rows[0].size // tail if n else 0
+    out = np.empty((n, n))
+    check(fn(prec, HOST, n, feat, rows.ctypes.data, out.ctypes.data, None))
+    return out
+
+
+def chi2_distance_matrix(hists, precision="fp32c"):
+    """(F, B) histograms -> (F, F) matrix of 1/2 sum (a-b)^2/(a+b) over bins
+    with a+b != 0 (construct_distance_matrix with distance_numpy,
+    CPET/utils/calculator.py:975-978, 1003-1015); zero diagonal."""
+    hists = hists if _is_torch(hists) else np.asarray(hists, np.float64)
+    if hists.ndim != 2:
+        raise ValueError("hists must be (n_histograms, n_bins)")
+    return _distance_matrix(lib().cpetgb_chi2_distance_matrix, hists, 1, precision)
+
+
+def field_distance_matrix(fields, precision="fp32c"):
+    """(F, P, 3) vector fields on one grid -> (F, F) matrix of sum_p |f_i[p] -
+    f_j[p]| (construct_distance_matrix_volume, CPET/utils/calculator.py:1042-1058)."""
+    fields = fields if _is_torch(fields) else np.asarray(fields, np.float64)
+    if fields.ndim != 3 or fields.shape[2] != 3:
+        raise ValueError("fields must be (n_fields, n_points, 3)")
+    return _distance_matrix(lib().cpetgb_field_distance_matrix, fields, 3, precision)

@@ -559,6 +559,89 @@ int hist_impl(int mem, int L, const double* result, int nb0, int nb1, const doub
   return CPETGB_OK;
 }
 
+int hist_sets_impl(int mem, int n_sets, const int64_t* offsets, const double* values, int nb0,
+                   int nb1, const double* range, uint64_t* counts, double* hists, void* stream) {
+  if (!valid_mem(mem)) return fail(CPETGB_EINVAL, "bad memory kind %d", mem);
+  if (n_sets < 0 || nb0 < 1 || nb1 < 1 || nb0 + nb1 > 4096)
+    return fail(CPETGB_EINVAL, "bad histogram shape (%d sets, %d x %d bins)", n_sets, nb0, nb1);
+  if (n_sets == 0) return CPETGB_OK;
+  if (!offsets || !range || (!counts && !hists)) return fail(CPETGB_EINVAL, "NULL pointer");
+  if (offsets[0] != 0) return fail(CPETGB_EINVAL, "offsets[0] must be 0");
+  int64_t max_set = 0;
+  for (int f = 0; f < n_sets; ++f) {
+    if (offsets[f + 1] < offsets[f]) return fail(CPETGB_EINVAL, "offsets decrease at set %d", f);
+    max_set = std::max(max_set, offsets[f + 1] - offsets[f]);
+  }
+  const int64_t L = offsets[n_sets];
+  if (L > 0 && !values) return fail(CPETGB_EINVAL, "values pointer is NULL");
+  for (int k = 0; k < 4; ++k)
+    if (!std::isfinite(range[k])) return fail(CPETGB_ERANGE, "histogram range must be finite");
+  if (range[0] > range[1] || range[2] > range[3])
+    return fail(CPETGB_ERANGE, "histogram range is inverted");
+  int rc;
+  Ctx* c = context(&rc);
+  if (!c) return rc;
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  if (mem == CPETGB_HOST && !s) s = c->stream;
+  Scratch S(s);
+  const size_t nbins = size_t(nb0) * nb1, total = nbins * size_t(n_sets);
+  const double* dv = values;
+  unsigned long long* dc = reinterpret_cast<unsigned long long*>(counts);
+  double* dh = hists;
+  double* de = nullptr;
+  int64_t* doff = nullptr;
+  if (mem == CPETGB_HOST && L) CK(h2d(const_cast<double**>(&dv), S, values, size_t(L) * 2), "copy values");
+  if (mem == CPETGB_HOST || !counts) CK(S.get(&dc, total), "alloc counts");
+  if (mem == CPETGB_HOST && hists) CK(S.get(&dh, total), "alloc histograms");
+  CK(S.get(&de, size_t(nb0 + nb1 + 2)), "alloc edges");
+  CK(h2d(&doff, S, offsets, size_t(n_sets) + 1), "copy offsets");
+  CK(cudaMemsetAsync(dc, 0, total * sizeof(unsigned long long), s), "zero counts");
+  CK(launch_hist2d_sets(n_sets, doff, max_set, dv, nb0, nb1, range, de, dc, hists ? dh : nullptr,
+                        c->status, s),
+     "histogram launch");
+  if (mem == CPETGB_HOST) {
+    if (counts)
+      CK(cudaMemcpyAsync(counts, dc, total * sizeof(uint64_t), cudaMemcpyDeviceToHost, s),
+         "copy counts");
+    if (hists)
+      CK(cudaMemcpyAsync(hists, dh, total * sizeof(double), cudaMemcpyDeviceToHost, s),
+         "copy histograms");
+    return finish(c, s);
+  }
+  return CPETGB_OK;
+}
+
+// kind 0: chi-square over histogram rows [n][feat]; kind 1: field rows [n][feat][3].
+int distance_impl(int kind, int prec, int mem, int n, int feat, const double* src, double* out,
+                  void* stream) {
+  if (!valid_prec(prec)) return fail(CPETGB_EINVAL, "bad precision %d", prec);
+  if (!valid_mem(mem)) return fail(CPETGB_EINVAL, "bad memory kind %d", mem);
+  if (n < 0 || feat < 0) return fail(CPETGB_EINVAL, "negative matrix or feature count");
+  if (n > 65535 * 64) return fail(CPETGB_EINVAL, "at most %d rows", 65535 * 64);
+  if (n == 0) return CPETGB_OK;
+  if (!out || (feat > 0 && !src)) return fail(CPETGB_EINVAL, "NULL pointer");
+  int rc;
+  Ctx* c = context(&rc);
+  if (!c) return rc;
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  if (mem == CPETGB_HOST && !s) s = c->stream;
+  Scratch S(s);
+  const size_t nc = kind == 0 ? 1 : 3;
+  const double* dsrc = src;
+  double* dout = out;
+  if (mem == CPETGB_HOST) {
+    if (feat) CK(h2d(const_cast<double**>(&dsrc), S, src, size_t(n) * feat * nc), "copy rows");
+    CK(S.get(&dout, size_t(n) * n), "alloc matrix");
+  }
+  CK(launch_distance_matrix(prec, kind, n, feat, dsrc, dout, s), "distance launch");
+  if (mem == CPETGB_HOST) {
+    CK(cudaMemcpyAsync(out, dout, size_t(n) * n * sizeof(double), cudaMemcpyDeviceToHost, s),
+       "copy matrix");
+    return finish(c, s);
+  }
+  return CPETGB_OK;
+}
+
 std::vector<double> widen(const float* p, size_t n) {
   std::vector<double> v(n);
   for (size_t i = 0; i < n; ++i) v[i] = p[i];
@@ -902,6 +985,23 @@ int cpetgb_plan_destroy(cpetgb_plan* plan) {
 int cpetgb_topo_hist2d(int mem, int n_lines, const double* result, int nb_dist, int nb_curv,
                        const double* range, uint64_t* counts, double* edges, void* stream) {
   return hist_impl(mem, n_lines, result, nb_dist, nb_curv, range, counts, edges, stream);
+}
+
+int cpetgb_topo_hist2d_sets(int mem, int n_sets, const int64_t* offsets, const double* values,
+                            int nb_dist, int nb_curv, const double* range, uint64_t* counts,
+                            double* hists, void* stream) {
+  return hist_sets_impl(mem, n_sets, offsets, values, nb_dist, nb_curv, range, counts, hists,
+                        stream);
+}
+
+int cpetgb_chi2_distance_matrix(int precision, int mem, int n, int bins, const double* hists,
+                                double* out, void* stream) {
+  return distance_impl(0, precision, mem, n, bins, hists, out, stream);
+}
+
+int cpetgb_field_distance_matrix(int precision, int mem, int n, int n_points,
+                                 const double* fields, double* out, void* stream) {
+  return distance_impl(1, precision, mem, n, n_points, fields, out, stream);
 }
 
 // ---- float32 drop-ins ----------------------------------------------------

@@ -13,6 +13,9 @@
 // A range bound given as NaN is taken from the data (min or max of that
 // column, as make_histograms does with np.min / np.max, lines 664-667); a
 // non-finite data bound sets the status word and no counts are produced.
+// The set form bins many value sets (one per .top file of make_histograms,
+// lines 689-711) with one binning in a single launch and can normalise each
+// set's counts to sum 1.
 #include <cmath>
 
 #include "common.cuh"
@@ -143,7 +146,93 @@ __global__ void __launch_bounds__(kBinThreads)
     if (sh[i]) atomicAdd(&counts[i], static_cast<unsigned long long>(sh[i]));
 }
 
+// Many value sets with one binning: set f = blockIdx.y holds the values
+// [off[f], off[f + 1]) and counts into counts[f][nb0 * nb1].
+__global__ void __launch_bounds__(kBinThreads)
+    hist_bin_sets_kernel(const int64_t* __restrict__ off, const double* __restrict__ vals, int nb0,
+                         int nb1, const double* __restrict__ edges,
+                         unsigned long long* __restrict__ counts, const int* __restrict__ status,
+                         int shared_bins) {
+  extern __shared__ unsigned char sraw[];
+  if (*status != kDevOk) return;
+  double* e0 = reinterpret_cast<double*>(sraw);
+  double* e1 = e0 + nb0 + 1;
+  unsigned int* sh = reinterpret_cast<unsigned int*>(e1 + nb1 + 1);
+  const int nbins = nb0 * nb1;
+  const int f = blockIdx.y;
+  const int64_t begin = off[f], end = off[f + 1];
+  unsigned long long* cf = counts + int64_t(f) * nbins;
+  for (int i = threadIdx.x; i <= nb0; i += blockDim.x) e0[i] = edges[i];
+  for (int i = threadIdx.x; i <= nb1; i += blockDim.x) e1[i] = edges[nb0 + 1 + i];
+  if (shared_bins)
+    for (int i = threadIdx.x; i < nbins; i += blockDim.x) sh[i] = 0u;
+  __syncthreads();
+  for (int64_t i = begin + blockIdx.x * int64_t(blockDim.x) + threadIdx.x; i < end;
+       i += int64_t(gridDim.x) * blockDim.x) {
+    const int b0 = bin_of(vals[2 * i], e0, nb0);
+    const int b1 = bin_of(vals[2 * i + 1], e1, nb1);
+    if (b0 < 0 || b1 < 0) continue;
+    if (shared_bins)
+      atomicAdd(&sh[b0 * nb1 + b1], 1u);
+    else
+      atomicAdd(&cf[b0 * nb1 + b1], 1ull);
+  }
+  if (!shared_bins) return;
+  __syncthreads();
+  for (int i = threadIdx.x; i < nbins; i += blockDim.x)
+    if (sh[i]) atomicAdd(&cf[i], static_cast<unsigned long long>(sh[i]));
+}
+
+// hists[f][b] = counts[f][b] / sum_b counts[f][b] in IEEE double: the integer
+// total is exact, so this is make_histograms' a / np.sum(a) bit for bit
+// (CPET/utils/calculator.py:709-711); an empty set gives NaN as numpy does.
+__global__ void __launch_bounds__(kBinThreads)
+    hist_normalise_kernel(int nbins, const unsigned long long* __restrict__ counts,
+                          double* __restrict__ hists) {
+  __shared__ unsigned long long red[kBinThreads / 32];
+  const int f = blockIdx.x;
+  const unsigned long long* cf = counts + int64_t(f) * nbins;
+  unsigned long long t = 0;
+  for (int i = threadIdx.x; i < nbins; i += blockDim.x) t += cf[i];
+  for (int o = 16; o >= 1; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = t;
+  __syncthreads();
+  unsigned long long total = 0;
+  for (int w = 0; w < kBinThreads / 32; ++w) total += red[w];
+  const double dt = static_cast<double>(total);
+  for (int i = threadIdx.x; i < nbins; i += blockDim.x)
+    hists[int64_t(f) * nbins + i] = __ddiv_rn(static_cast<double>(cf[i]), dt);
+}
+
 }  // namespace
+
+// Many sets, one binning: range {lo0, hi0, lo1, hi1} finite (host); d_off the
+// device copy of the set offsets [n_sets + 1]; counts [n_sets][nb0*nb1] zeroed;
+// hists (optional) receives the normalised histograms.
+cudaError_t launch_hist2d_sets(int n_sets, const int64_t* d_off, int64_t max_set,
+                               const double* vals, int nb0, int nb1, const double* range,
+                               double* edges, unsigned long long* counts, double* hists,
+                               int* status, cudaStream_t s) {
+  if (n_sets <= 0) return cudaSuccess;
+  hist_range_kernel<<<1, kRangeThreads, 0, s>>>(0, vals, nb0, nb1, range[0], range[1], range[2],
+                                                range[3], edges, status);
+  cudaError_t err = cudaGetLastError();
+  if (err != cudaSuccess) return err;
+  const int nbins = nb0 * nb1;
+  size_t smem = sizeof(double) * (nb0 + nb1 + 2);
+  const int shared_bins =
+      (nbins <= kMaxSharedBins && smem + sizeof(unsigned int) * nbins <= 48 * 1024) ? 1 : 0;
+  if (shared_bins) smem += sizeof(unsigned int) * nbins;
+  if (smem > 48 * 1024) return cudaErrorInvalidValue;  // callers keep nb0 + nb1 <= 4096
+  const int64_t per = (max_set + kBinThreads * 4 - 1) / (kBinThreads * 4);
+  const int bx = static_cast<int>(per < 1 ? 1 : (per > 64 ? 64 : per));
+  hist_bin_sets_kernel<<<dim3(bx, n_sets), kBinThreads, smem, s>>>(d_off, vals, nb0, nb1, edges,
+                                                                   counts, status, shared_bins);
+  err = cudaGetLastError();
+  if (err != cudaSuccess || !hists) return err;
+  hist_normalise_kernel<<<n_sets, kBinThreads, 0, s>>>(nbins, counts, hists);
+  return cudaGetLastError();
+}
 
 // range: {lo0, hi0, lo1, hi1} on the host; NaN = from the data.
 // counts (nb0*nb1, row-major over (distance bin, curvature bin)) must be zeroed.

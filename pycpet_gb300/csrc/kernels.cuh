@@ -150,5 +150,14 @@ void tuned_grid_shape(int prec, int kind, double pair_evals, int* ppt, int* item
 cudaError_t launch_hist2d(int n, const double* vals, int nb0, int nb1, const double* range,
                           double* edges, unsigned long long* counts, int* status,
                           cudaStream_t s);
+cudaError_t launch_hist2d_sets(int n_sets, const int64_t* d_off, int64_t max_set,
+                               const double* vals, int nb0, int nb1, const double* range,
+                               double* edges, unsigned long long* counts, double* hists,
+                               int* status, cudaStream_t s);
+
+// distance.cu: kind 0 = chi-square over histogram rows [n][feat]; kind 1 =
+// summed Euclidean norms over field rows [n][feat][3]; out [n][n].
+cudaError_t launch_distance_matrix(int prec, int kind, int n, int feat, const double* src,
+                                   double* out, cudaStream_t s);
 
 }  // namespace cpetgb

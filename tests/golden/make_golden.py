@@ -21,6 +21,11 @@ Fixtures written (all small, compressed .npz):
   examples_topology.npz     the (distance, curvature) rows of example 3A's
                             shipped .top files and the reference's
                             make_histograms of them
+  ref_cluster.npz           ten synthetic .top files (900 rows each) through
+                            the reference's make_histograms and
+                            construct_distance_matrix, and eight synthetic
+                            vector fields (343 points) through its
+                            construct_distance_matrix_volume
 """
 from __future__ import annotations
 
@@ -59,7 +64,7 @@ def _stub_modules():
     mod("kneed", KneeLocator=object)
     tl = mod("tensorly")
     tl.decomposition = mod("tensorly.decomposition", parafac=None)
-    mod("pandas")
+    mod("pandas", DataFrame=type("DataFrame", (), {}), Series=type("Series", (), {}))  # sklearn type checks
     mod("seaborn")
 
 
@@ -159,6 +164,29 @@ def examples_topology(ref_root, ucalc, out):
     np.savez_compressed(out, **rec)
 
 
+def ref_cluster(ucalc, out):
+    import tempfile
+
+    rng = np.random.default_rng(21)
+    sets = []
+    for f in range(10):  # (distance, curvature) rows shaped like streamline output
+        d = np.clip(rng.gamma(2.0 + 0.2 * f, 0.6, 900), 0.0, 5.2)
+        c = rng.lognormal(0.3 + 0.05 * f, 0.8, 900)
+        sets.append(np.column_stack([d, c]))
+    with tempfile.TemporaryDirectory() as tmp:
+        files = []
+        for f, v in enumerate(sets):
+            path = os.path.join(tmp, f"frame_{f:02d}.top")
+            np.savetxt(path, v)
+            files.append(path)
+        hists = ucalc.make_histograms(files)
+    dmat = ucalc.construct_distance_matrix(hists)
+    fields = [rng.normal(0.0, 1.0 + 0.1 * f, (343, 3)) for f in range(8)]
+    vmat = ucalc.construct_distance_matrix_volume(fields)
+    np.savez_compressed(out, values=np.concatenate(sets), offsets=np.arange(11) * 900, hists=hists,
+                        dmat=dmat, fields=np.stack(fields), vmat=vmat)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--ref", default="/root/reference")
@@ -168,6 +196,7 @@ def main():
     ref_grid(ucalc, os.path.join(HERE, "ref_grid.npz"))
     ref_topo(scalc, os.path.join(HERE, "ref_topo.npz"))
     examples_topology(a.ref, ucalc, os.path.join(HERE, "examples_topology.npz"))
+    ref_cluster(ucalc, os.path.join(HERE, "ref_cluster.npz"))
     for f in sorted(glob.glob(os.path.join(HERE, "*.npz"))):
         print(f, os.path.getsize(f))
 

@@ -101,3 +101,23 @@ def test_reference_library_cross_check(oracle):
     ref.thread_operation(len(q), 200, np.float32(0.01), pts[0].copy(), dims, x, q, ret)
     r64, _, _ = oracle.topo_lines_f64(pts[:1], [200], x, q, 0.01, dims)
     assert abs(r64[0, 0] - ret[0]) < 5e-6
+
+
+def test_cluster_oracle_matches_reference(golden, oracle):
+    """construct_distance_matrix / construct_distance_matrix_volume: the C
+    restatement against the reference's own outputs; make_histograms' binning
+    rule (Freedman-Diaconis bin counts, global range, numpy histogram2d,
+    division by each file's total) restated on the host reproduces the
+    reference's histograms bit for bit."""
+    from pycpet_gb300.calculator import histogram_bins
+
+    c = golden("ref_cluster.npz")
+    np.testing.assert_allclose(oracle.chi2_matrix_f64(c["hists"]), c["dmat"], rtol=1e-13, atol=0)
+    np.testing.assert_allclose(oracle.field_matrix_f64(c["fields"]), c["vmat"], rtol=1e-13, atol=0)
+    v, off = c["values"], c["offsets"]
+    bins, rng = histogram_bins(v[:, 0], v[:, 1], off[1] - off[0])
+    rows = []
+    for f in range(len(off) - 1):
+        h = oracle.histogram2d(v[off[f]:off[f + 1], 0], v[off[f]:off[f + 1], 1], bins, rng)
+        rows.append((h / np.sum(h)).flatten())
+    np.testing.assert_array_equal(np.array(rows), c["hists"])
