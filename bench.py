@@ -180,7 +180,7 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-extras", action="store_true", help="skip the FP64 / grid / CPU comparison legs")
     ap.add_argument("--lines", type=int, default=N_LINES, help="streamlines per step (smaller cases for ncu)")
-    ap.add_argument("--workload", default="topo", choices=["topo", "grid", "topo-batch", "serve"],
+    ap.add_argument("--workload", default="topo", choices=["topo", "grid", "topo-batch", "serve", "cluster"],
                     help="grid: the 64-frame batched volume + volume_ESP workload; topo-batch: "
                          "frames of 5,000-20,000 charges with uneven line counts in one launch")
     ap.add_argument("--requests", type=int, default=400, help="serve: number of requests")
@@ -220,6 +220,8 @@ def main():
         return topo_batch_main(args, rank, world, dev, torch, dist)
     if args.workload == "serve":
         return serve_main(args, rank, world, dev, torch, dist)
+    if args.workload == "cluster":
+        return cluster_main(args, rank, world, dev, torch, dist)
     x, q, starts, caps = make_inputs(rank)
     if args.lines != N_LINES:
         starts, caps = starts[:args.lines], caps[:args.lines]
@@ -458,6 +460,88 @@ def serve_main(args, rank, world, dev, torch, dist):
     out["serving"] = results
     out["latency_ms"] = {"p50": results["fp32c"]["latency"]["all"]["p50_ms"],
                          "p99": results["fp32c"]["latency"]["all"]["p99_ms"]}
+    if rank == 0:
+        print(json.dumps(out), flush=True)
+    if world > 1:
+        dist.destroy_process_group()
+
+
+def cluster_inputs(rank, n_hist=4096, n_fields=1024):
+    """Synthetic trajectory-scale clustering inputs: n_hist topology histograms
+    of 20 x 20 bins (rows normalised to 1, about a third of the bins empty) and
+    n_fields vector fields on a 21^3 grid."""
+    rng = np.random.default_rng(7070 + rank)
+    base = rng.gamma(1.0, 1.0, 400) * (rng.random(400) < 0.7)
+    h = base * rng.lognormal(0.0, 0.3, (n_hist, 400))
+    h /= h.sum(axis=1, keepdims=True)
+    fld = rng.normal(0.0, 1.0, (9261, 3)) + rng.normal(0.0, 0.2, (n_fields, 9261, 3))
+    return h, fld
+
+
+def cluster_main(args, rank, world, dev, torch, dist):
+    """--workload cluster: the chi-square distance matrix of 4,096 topology
+    histograms (20 x 20 bins) and the field distance matrix of 1,024 vector
+    fields on a 21^3 grid, device-resident (FP32C and FP64), against the
+    oracle's C restatement of construct_distance_matrix(_volume) on all host
+    cores over a sample of rows."""
+    from pycpet_gb300 import _lib, chi2_distance_matrix, field_distance_matrix
+
+    h, fld = cluster_inputs(rank)
+    dh, df = torch.from_numpy(h).to(dev), torch.from_numpy(fld).to(dev)
+    flush = torch.empty(L2_FLUSH_BYTES, dtype=torch.uint8, device=dev)
+    mufu = _lib.measure_peak(2)
+
+    def timed(fn, arg, prec):
+        for _ in range(args.warmup):
+            fn(arg, prec)
+        torch.cuda.synchronize()
+        ts = []
+        for k in range(args.steps):
+            flush.fill_(k & 0xFF)
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            fn(arg, prec)
+            e1.record()
+            torch.cuda.synchronize()
+            ts.append(e0.elapsed_time(e1) * 1e-3)
+        return statistics.median(ts)
+
+    n_h, n_f = h.shape[0], fld.shape[0]
+    terms_h = n_h * (n_h - 1) // 2 * h.shape[1]
+    terms_f = n_f * (n_f - 1) // 2 * fld.shape[1]
+    res = {}
+    for prec in ("fp32c", "fp64"):
+        th = timed(chi2_distance_matrix, dh, prec)
+        tf = timed(field_distance_matrix, df, prec)
+        res[prec] = {"chi2_terms_per_s": terms_h / th, "chi2_ms": th * 1e3,
+                     "field_terms_per_s": terms_f / tf, "field_ms": tf * 1e3}
+    d32 = chi2_distance_matrix(dh[:512], "fp32c").cpu().numpy()
+    d64 = chi2_distance_matrix(dh[:512], "fp64").cpu().numpy()
+    err = float(np.max(np.abs(d32 - d64)) / np.max(d64))
+    out = {"metric": "chi-square distance-matrix terms/s (histogram pairs x bins)",
+           "value": res["fp32c"]["chi2_terms_per_s"], "unit": "terms/s", "n_gpus": world,
+           "steps": args.steps, "warmup": args.warmup, "ms_per_step": res["fp32c"]["chi2_ms"],
+           "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+           "data": "synthetic (seeded)",
+           "config": {"workload": f"construct_distance_matrix of {n_h} histograms x 400 bins; "
+                                  f"construct_distance_matrix_volume of {n_f} fields x 9,261 points",
+                      "l2": "flushed between timed steps"},
+           "forms": res, "fp32c_vs_fp64_max_rel_err_512": err,
+           "roofline": {"bound": "mufu", "achieved": res["fp32c"]["chi2_terms_per_s"] / 1e12, "peak": mufu / 1e12,
+                        "unit": "Tterm/s", "frac": res["fp32c"]["chi2_terms_per_s"] / mufu,
+                        "note": "one MUFU reciprocal per chi-square term; peak = MUFU rsqrt rate measured now"}}
+    if rank == 0 and world == 1:
+        from oracle import oracle
+
+        threads = os.cpu_count() or 1
+        t0 = time.perf_counter()
+        oracle.chi2_matrix_f64(h[:768], threads=threads)
+        t1 = time.perf_counter()
+        oracle.field_matrix_f64(fld[:128], threads=threads)
+        t2 = time.perf_counter()
+        out["cpu_baseline"] = {"value": 768 * 767 // 2 * 400 / (t1 - t0), "unit": "terms/s", "cores": threads,
+                               "kind": "port", "field_terms_per_s": 128 * 127 // 2 * 9261 / (t2 - t1),
+                               "sample": "first 768 histograms / first 128 fields, oracle C restatement (FP64)"}
     if rank == 0:
         print(json.dumps(out), flush=True)
     if world > 1:

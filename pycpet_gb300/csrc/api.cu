@@ -633,7 +633,10 @@ int distance_impl(int kind, int prec, int mem, int n, int feat, const double* sr
     if (feat) CK(h2d(const_cast<double**>(&dsrc), S, src, size_t(n) * feat * nc), "copy rows");
     CK(S.get(&dout, size_t(n) * n), "alloc matrix");
   }
-  CK(launch_distance_matrix(prec, kind, n, feat, dsrc, dout, s), "distance launch");
+  const int splits = distance_splits(n, feat, c->sms);
+  double* partial = nullptr;
+  if (splits > 1) CK(S.get(&partial, size_t(splits) * n * n), "alloc partial sums");
+  CK(launch_distance_matrix(prec, kind, n, feat, dsrc, dout, splits, partial, s), "distance launch");
   if (mem == CPETGB_HOST) {
     CK(cudaMemcpyAsync(out, dout, size_t(n) * n * sizeof(double), cudaMemcpyDeviceToHost, s),
        "copy matrix");

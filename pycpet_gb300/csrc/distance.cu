@@ -13,7 +13,10 @@
 // Both are symmetric with a zero diagonal.
 //
 // One CTA computes a 64 x 64 tile of the upper triangle (tiles below the
-// diagonal return at once) and writes it and its mirror image.  The features
+// diagonal return at once) and writes it and its mirror image.  When there are
+// too few tiles to fill the GPU (fewer than about four per SM) the features are
+// split over several CTAs per tile whose partial sums are added afterwards in
+// split order, so the result does not depend on scheduling.  The features
 // (histogram bins or grid points) stream through shared memory in chunks of
 // 32 bins or 8-16 points, transposed so that for one feature a thread reads
 // its 4 rows and 4 columns as broadcast loads; each thread owns 4 x 4 matrix
@@ -27,6 +30,7 @@
 //          into a running (sum, compensation) pair.
 // The term of (i, j) equals the term of (j, i) bit for bit in both forms, so
 // a tile on the diagonal writes an exactly symmetric block.
+#include <algorithm>
 #include <cstdint>
 
 #include "common.cuh"
@@ -38,8 +42,8 @@ namespace {
 constexpr int kTile = 64;      // matrix rows / columns per CTA
 constexpr int kThreads = 256;  // 16 x 16 threads, 4 x 4 entries each
 
-// Features staged per step: 32 histogram bins, 16 (FP32) or 8 (FP64) grid
-// points of 3 components, keeping both staged tiles under 48 KB.
+// Features staged per step: 32 histogram bins, or 16 (FP32) / 8 (FP64) grid
+// points, keeping both staged tiles at or under 33 KB.
 template <typename Real, int NC>
 constexpr int chunk_of() {
   return NC == 1 ? 32 : (sizeof(Real) == 4 ? 16 : 8);
@@ -66,6 +70,20 @@ struct Acc<float> {
   __device__ double value() const { return static_cast<double>(s) - static_cast<double>(c); }
 };
 
+// One staged feature of one row: a histogram bin, or a grid point's vector
+// padded to 4 components so that it is a single (FP32) or double (FP64)
+// vector load.
+template <typename Real, int NC>
+struct Feat;
+template <typename Real>
+struct Feat<Real, 1> {
+  Real v;
+};
+template <typename Real>
+struct alignas(4 * sizeof(Real)) Feat<Real, 3> {
+  Real x, y, z, w;
+};
+
 __device__ __forceinline__ double chi2_term(double a, double b) {
   const double s = __dadd_rn(a, b);
   const double d = __dsub_rn(a, b);
@@ -78,47 +96,62 @@ __device__ __forceinline__ float chi2_term(float a, float b) {
   return __fmul_rn(__fmul_rn(d, d), r);
 }
 
-__device__ __forceinline__ double norm_term(double ax, double ay, double az, double bx, double by,
-                                            double bz) {
-  const double dx = __dsub_rn(ax, bx), dy = __dsub_rn(ay, by), dz = __dsub_rn(az, bz);
+template <typename Real>
+__device__ __forceinline__ Real term(const Feat<Real, 1>& a, const Feat<Real, 1>& b) {
+  return chi2_term(a.v, b.v);
+}
+__device__ __forceinline__ double term(const Feat<double, 3>& a, const Feat<double, 3>& b) {
+  const double dx = __dsub_rn(a.x, b.x), dy = __dsub_rn(a.y, b.y), dz = __dsub_rn(a.z, b.z);
   return sqrt(__dadd_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)), __dmul_rn(dz, dz)));
 }
-__device__ __forceinline__ float norm_term(float ax, float ay, float az, float bx, float by,
-                                           float bz) {
-  const float dx = __fsub_rn(ax, bx), dy = __fsub_rn(ay, by), dz = __fsub_rn(az, bz);
+__device__ __forceinline__ float term(const Feat<float, 3>& a, const Feat<float, 3>& b) {
+  const float dx = __fsub_rn(a.x, b.x), dy = __fsub_rn(a.y, b.y), dz = __fsub_rn(a.z, b.z);
   const float r2 = __fmaf_rn(dz, dz, __fmaf_rn(dy, dy, __fmul_rn(dx, dx)));
   return __fmul_rn(r2, rsqrt_mufu(fmaxf(r2, 1e-37f)));  // r2 == 0 gives 0
 }
 
+template <typename Real, int NC>
+__device__ __forceinline__ void load_feat(Feat<Real, NC>& f, const double* p, bool ok) {
+  if constexpr (NC == 1) {
+    f.v = ok ? static_cast<Real>(p[0]) : Real(0);
+  } else {
+    f.x = ok ? static_cast<Real>(p[0]) : Real(0);
+    f.y = ok ? static_cast<Real>(p[1]) : Real(0);
+    f.z = ok ? static_cast<Real>(p[2]) : Real(0);
+    f.w = Real(0);
+  }
+}
+
 // KIND 0: chi2 over `feat` bins of rows of `src` ([n][feat] doubles).
 // KIND 1: field norm over `feat` points of rows of `src` ([n][feat][3] doubles).
+// blockIdx.z = feature split: features [z * per, min(feat, (z+1) * per)).
+// With one split the CTA writes the final matrix (halved for chi2, zero
+// diagonal); with several it writes its partial sums to part[z][n][n].
 template <typename Real, int KIND>
 __global__ void __launch_bounds__(kThreads)
-    distance_kernel(int n, int feat, const double* __restrict__ src, double* __restrict__ out) {
+    distance_kernel(int n, int feat, int per, const double* __restrict__ src,
+                    double* __restrict__ out, double* __restrict__ part_out) {
   constexpr int NC = KIND == 0 ? 1 : 3;  // components per feature
   constexpr int kChunk = chunk_of<Real, NC>();
+  using F = Feat<Real, NC>;
   const int ib = blockIdx.y, jb = blockIdx.x;
   if (ib > jb) return;  // lower triangle: the mirror of a computed tile
-  __shared__ Real sA[NC][kChunk][kTile + 1];
-  __shared__ Real sB[NC][kChunk][kTile + 1];
+  __shared__ F sA[kChunk][kTile + 1];
+  __shared__ F sB[kChunk][kTile + 1];
   const int tid = threadIdx.x, tx = tid & 15, ty = tid >> 4;
   const int i0 = ib * kTile, j0 = jb * kTile;
   const int64_t row_len = int64_t(feat) * NC;
+  const int kb = blockIdx.z * per, ke = min(feat, kb + per);
 
   Acc<Real> acc[4][4];
-  for (int k0 = 0; k0 < feat; k0 += kChunk) {
+  for (int k0 = kb; k0 < ke; k0 += kChunk) {
     __syncthreads();  // previous chunk consumed
-    // stage rows i0.. and j0.. for features k0 .. k0+kChunk-1 (zero outside the matrix)
-    for (int e = tid; e < kTile * kChunk * NC; e += kThreads) {
-      const int comp = e % NC, k = (e / NC) % kChunk, row = e / (NC * kChunk);
-      const int kk = k0 + k;
-      double va = 0.0, vb = 0.0;
-      if (kk < feat) {
-        if (i0 + row < n) va = src[(i0 + row) * row_len + int64_t(kk) * NC + comp];
-        if (j0 + row < n) vb = src[(j0 + row) * row_len + int64_t(kk) * NC + comp];
-      }
-      sA[comp][k][row] = static_cast<Real>(va);
-      sB[comp][k][row] = static_cast<Real>(vb);
+    // stage rows i0.. and j0.. for features k0 .. k0+kChunk-1 (zero outside)
+    for (int e = tid; e < kTile * kChunk; e += kThreads) {
+      const int k = e % kChunk, row = e / kChunk, kk = k0 + k;
+      const bool in = kk < ke;
+      load_feat<Real, NC>(sA[k][row], src + (i0 + row) * row_len + int64_t(kk) * NC, in && i0 + row < n);
+      load_feat<Real, NC>(sB[k][row], src + (j0 + row) * row_len + int64_t(kk) * NC, in && j0 + row < n);
     }
     __syncthreads();
     Real part[4][4];
@@ -126,26 +159,20 @@ __global__ void __launch_bounds__(kThreads)
     for (int r = 0; r < 4; ++r)
 #pragma unroll
       for (int c = 0; c < 4; ++c) part[r][c] = Real(0);
-    const int kn = min(kChunk, feat - k0);
+    const int kn = min(kChunk, ke - k0);
 #pragma unroll 4
     for (int k = 0; k < kn; ++k) {
-      Real a[NC][4], b[NC][4];
+      F a[4], b[4];
 #pragma unroll
-      for (int q = 0; q < NC; ++q)
-#pragma unroll
-        for (int r = 0; r < 4; ++r) {
-          a[q][r] = sA[q][k][ty + 16 * r];
-          b[q][r] = sB[q][k][tx + 16 * r];
-        }
+      for (int r = 0; r < 4; ++r) {
+        a[r] = sA[k][ty + 16 * r];
+        b[r] = sB[k][tx + 16 * r];
+      }
 #pragma unroll
       for (int r = 0; r < 4; ++r)
 #pragma unroll
         for (int c = 0; c < 4; ++c) {
-          Real t;
-          if constexpr (KIND == 0)
-            t = chi2_term(a[0][r], b[0][c]);
-          else
-            t = norm_term(a[0][r], a[1][r], a[2][r], b[0][c], b[1][c], b[2][c]);
+          const Real t = term(a[r], b[c]);
           if constexpr (sizeof(Real) == 8)
             part[r][c] = __dadd_rn(part[r][c], t);
           else
@@ -158,6 +185,7 @@ __global__ void __launch_bounds__(kThreads)
       for (int c = 0; c < 4; ++c) acc[r][c].add(part[r][c]);
   }
 
+  double* dst = part_out ? part_out + int64_t(blockIdx.z) * n * n : out;
 #pragma unroll
   for (int r = 0; r < 4; ++r)
 #pragma unroll
@@ -165,31 +193,65 @@ __global__ void __launch_bounds__(kThreads)
       const int i = i0 + ty + 16 * r, j = j0 + tx + 16 * c;
       if (i >= n || j >= n) continue;
       double v = acc[r][c].value();
-      if (KIND == 0) v *= 0.5;
-      if (i == j) v = 0.0;
-      out[int64_t(i) * n + j] = v;
-      if (ib != jb) out[int64_t(j) * n + i] = v;
+      if (!part_out) {
+        if (KIND == 0) v *= 0.5;
+        if (i == j) v = 0.0;
+      }
+      dst[int64_t(i) * n + j] = v;
+      if (ib != jb) dst[int64_t(j) * n + i] = v;
     }
+}
+
+// Sum of the feature splits in split order (deterministic); chi2 halved;
+// zero diagonal.
+__global__ void distance_reduce_kernel(int kind, int n, int splits, const double* __restrict__ part,
+                                       double* __restrict__ out) {
+  const int64_t nn = int64_t(n) * n;
+  for (int64_t e = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; e < nn;
+       e += int64_t(gridDim.x) * blockDim.x) {
+    double v = part[e];
+    for (int z = 1; z < splits; ++z) v = __dadd_rn(v, part[z * nn + e]);
+    if (kind == 0) v *= 0.5;
+    if (e / n == e % n) v = 0.0;
+    out[e] = v;
+  }
 }
 
 }  // namespace
 
+int distance_splits(int n, int feat, int num_sms) {
+  const int nb = (n + kTile - 1) / kTile;
+  const int64_t tiles = int64_t(nb) * (nb + 1) / 2;
+  const int64_t want = 4LL * num_sms;  // about four CTAs per SM
+  if (tiles >= want || feat < 256) return 1;
+  int s = static_cast<int>((want + tiles - 1) / tiles);
+  return std::max(1, std::min(s, feat / 64));  // at least 64 features per split
+}
+
 cudaError_t launch_distance_matrix(int prec, int kind, int n, int feat, const double* src,
-                                   double* out, cudaStream_t s) {
+                                   double* out, int splits, double* partial, cudaStream_t s) {
   if (n <= 0) return cudaSuccess;
   const int nb = (n + kTile - 1) / kTile;
-  const dim3 grid(nb, nb);
+  if (splits < 1 || feat == 0) splits = 1;
+  const int per = (feat + splits - 1) / splits;
+  double* pout = splits > 1 ? partial : nullptr;
+  const dim3 grid(nb, nb, splits);
   if (prec == kFP64) {
     if (kind == 0)
-      distance_kernel<double, 0><<<grid, kThreads, 0, s>>>(n, feat, src, out);
+      distance_kernel<double, 0><<<grid, kThreads, 0, s>>>(n, feat, per, src, out, pout);
     else
-      distance_kernel<double, 1><<<grid, kThreads, 0, s>>>(n, feat, src, out);
+      distance_kernel<double, 1><<<grid, kThreads, 0, s>>>(n, feat, per, src, out, pout);
   } else {
     if (kind == 0)
-      distance_kernel<float, 0><<<grid, kThreads, 0, s>>>(n, feat, src, out);
+      distance_kernel<float, 0><<<grid, kThreads, 0, s>>>(n, feat, per, src, out, pout);
     else
-      distance_kernel<float, 1><<<grid, kThreads, 0, s>>>(n, feat, src, out);
+      distance_kernel<float, 1><<<grid, kThreads, 0, s>>>(n, feat, per, src, out, pout);
   }
+  cudaError_t err = cudaGetLastError();
+  if (err != cudaSuccess || splits == 1) return err;
+  const int64_t nn = int64_t(n) * n;
+  const int blocks = static_cast<int>(std::min<int64_t>((nn + 255) / 256, 4096));
+  distance_reduce_kernel<<<blocks, 256, 0, s>>>(kind, n, splits, partial, out);
   return cudaGetLastError();
 }
 

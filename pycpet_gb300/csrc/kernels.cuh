@@ -157,7 +157,9 @@ cudaError_t launch_hist2d_sets(int n_sets, const int64_t* d_off, int64_t max_set
 
 // distance.cu: kind 0 = chi-square over histogram rows [n][feat]; kind 1 =
 // summed Euclidean norms over field rows [n][feat][3]; out [n][n].
+// splits > 1 (distance_splits) needs partial scratch of splits * n * n doubles.
+int distance_splits(int n, int feat, int num_sms);
 cudaError_t launch_distance_matrix(int prec, int kind, int n, int feat, const double* src,
-                                   double* out, cudaStream_t s);
+                                   double* out, int splits, double* partial, cudaStream_t s);
 
 }  // namespace cpetgb
