@@ -86,6 +86,11 @@ int cpetgb_calc_field(float* E, const float* x_init, int n_charges, const float*
 int cpetgb_thread_operation(int n_charges, int n_iter, float step_size, const float* x_0,
                             const float* dimensions, const float* x, const float* Q,
                             float* ret);
+/* thread_operation_dipole: math_module.c:593-659, c_ops.py:96-110,304-325
+ * (dipole moments mu[n_dipoles][3] instead of charges). */
+int cpetgb_thread_operation_dipole(int n_dipoles, int n_iter, float step_size, const float* x_0,
+                                   const float* dimensions, const float* x, const float* mu,
+                                   float* ret);
 /* All lines of compute_topo_complete_c_shared (CPET/source/calculator.py:675-712)
  * in one call: x_0[L][3], n_iter[L], ret[L][2] in start order. */
 int cpetgb_thread_operation_batch(int n_lines, int n_charges, const int32_t* n_iter,
@@ -117,6 +122,15 @@ int cpetgb_topo_lines(int precision, int mem, int n_lines, int n_charges, const 
                       const int32_t* n_iter, double step, const double* half_dims,
                       const double* x, const double* q, double* result, double* ends,
                       int32_t* steps, void* stream);
+/* Streamlines through the field of point dipoles (thread_operation_dipole,
+ * CPET/utils/math_module.c:593-659, with the term of calc_field_base_dipole,
+ * 335-371: r^-5 ((3 mu_x R_x + mu_y R_y + mu_z R_z) R - mu r^2), the factor 3
+ * on the x term as the reference writes it).  mu[n_dipoles][3]; everything else
+ * as cpetgb_topo_lines. */
+int cpetgb_topo_dipole_lines(int precision, int mem, int n_lines, int n_dipoles,
+                             const double* starts, const int32_t* n_iter, double step,
+                             const double* half_dims, const double* x, const double* mu,
+                             double* result, double* ends, int32_t* steps, void* stream);
 /* Streamlines of many frames in one persistent launch.  desc is a HOST array
  * [n_frames][4] of int64 {charge_offset, n_charges, line_offset, n_lines} into
  * x/q and starts/n_iter/result/ends/steps; params is a HOST array

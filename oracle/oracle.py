@@ -12,6 +12,8 @@ oracle_ref32.c by oracle/Makefile) and exposes numpy-level wrappers:
   the timed CPU baseline ("port").
 * ``histogram2d``: numpy's own histogram2d, the function the reference calls in
   make_histograms (CPET/utils/calculator.py:702-707).
+* ``topo_lines_dipole``: thread_operation_dipole (math_module.c:593-659),
+  FP64 or the reference's float arithmetic.
 * ``chi2_matrix_f64`` / ``field_matrix_f64``: the clustering distance matrices
   construct_distance_matrix (calculator.py:975-978, 1003-1015) and
   construct_distance_matrix_volume (calculator.py:1042-1058) in IEEE double.
@@ -59,6 +61,9 @@ def lib():
             _c_int, _c_int, _i, ctypes.c_float, _f, _f, _f, _f, _f, _f, _i, _c_int]
         L.oracle_chi2_matrix_f64.argtypes = [_c_int, _c_int, _d, _d, _c_int]
         L.oracle_field_matrix_f64.argtypes = [_c_int, _c_int, _d, _d, _c_int]
+        _v = ctypes.c_void_p
+        L.oracle_topo_lines_dipole_mt.argtypes = [_c_int, _c_int, _c_int, _i, ctypes.c_double, _v, _v, _v, _v,
+                                                  _v, _v, _i, _c_int]
         _LIB = L
     return _LIB
 
@@ -161,6 +166,23 @@ def field_matrix_f64(fields, threads=None):
     return out
 
 
+def topo_lines_dipole(x0, n_iter, x, mu, step, dims, f32=False, threads=None):
+    """thread_operation_dipole (CPET/utils/math_module.c:593-659) for every start
+    point: FP64 (f32=False) or the reference's float arithmetic (f32=True).
+    Returns (ret (L,2) = [dist, curv], ends (L,3), steps (L,))."""
+    dt = np.float32 if f32 else np.float64
+    x0 = _c(x0, dt).reshape(-1, 3)
+    L = len(x0)
+    n_iter = _c(np.broadcast_to(np.asarray(n_iter), (L,)), np.int32)
+    x, mu, dims = _c(x, dt).reshape(-1, 3), _c(mu, dt).reshape(-1, 3), _c(dims, dt).reshape(3)
+    ret, ends = np.empty((L, 2), dtype=dt), np.empty((L, 3), dtype=dt)
+    steps = np.empty(L, dtype=np.int32)
+    p = lambda a: a.ctypes.data
+    lib().oracle_topo_lines_dipole_mt(int(f32), L, len(mu), n_iter, float(np.float32(step) if f32 else step),
+                                      p(x0), p(dims), p(x), p(mu), p(ret), p(ends), steps, _threads(threads))
+    return ret, ends, steps
+
+
 def load_reference():
     """The reference's own C library built from source into oracle/_ref, or None."""
     so = os.path.join(HERE, "_ref", "math_module.so")
@@ -178,4 +200,6 @@ def load_reference():
     L.calc_field.restype = None
     L.thread_operation.argtypes = [_c_int, _c_int, ctypes.c_float, f1, f1, f2, f1, f1]
     L.thread_operation.restype = None
+    L.thread_operation_dipole.argtypes = [_c_int, _c_int, ctypes.c_float, f1, f1, f2, f2, f1]
+    L.thread_operation_dipole.restype = None
     return L

@@ -136,3 +136,67 @@ int oracle_topo_line_f32(int N, int n_iter, float h, const float x0[3], const fl
   return steps;
 }
 
+
+/* calc_field_base_dipole (math_module.c:335-371) in the reference's
+ * arithmetic: float R, r from a double sqrt of double squares, r^2 and r^-5
+ * through double pow rounded to float, float products and sums; the factor 3
+ * on the x term only, as written there. */
+static void dipole_field_f32(const float p[3], int N, const float* x, const float* mu, float E[3]) {
+  const float k = 14.3996451f;
+  float ex = 0.f, ey = 0.f, ez = 0.f;
+  for (int j = 0; j < N; ++j) {
+    float R0 = p[0] - x[3 * j], R1 = p[1] - x[3 * j + 1], R2 = p[2] - x[3 * j + 2];
+    float rn = (float)sqrt(pow(R0, 2) + pow(R1, 2) + pow(R2, 2));
+    float r2 = (float)pow(rn, 2);
+    float r5 = (float)pow(rn, -5);
+    const float* m = mu + 3 * j;
+    float dot = 3 * m[0] * R0 + m[1] * R1 + m[2] * R2;
+    ex += k * r5 * (dot * R0 - m[0] * r2);
+    ey += k * r5 * (dot * R1 - m[1] * r2);
+    ez += k * r5 * (dot * R2 - m[2] * r2);
+  }
+  E[0] = ex;
+  E[1] = ey;
+  E[2] = ez;
+}
+
+static void dipole_step_f32(const float p[3], int N, const float* x, const float* mu, float h,
+                            float out[3]) {
+  float E[3];
+  dipole_field_f32(p, N, x, mu, E);
+  float n = (float)sqrt(pow(E[0], 2) + pow(E[1], 2) + pow(E[2], 2));
+  for (int k = 0; k < 3; ++k) out[k] = p[k] + h * E[k] / n;
+}
+
+/* thread_operation_dipole (math_module.c:593-659) in the reference's float arithmetic. */
+int oracle_topo_line_dipole_f32(int N, int n_iter, float h, const float x0[3], const float dims[3],
+                                const float* x, const float* mu, float ret[2], float end[3]) {
+  float cur[3] = {x0[0], x0[1], x0[2]};
+  int steps = 0;
+  for (int i = 0; i < n_iter; ++i) {
+    float nxt[3];
+    dipole_step_f32(cur, N, x, mu, h, nxt);
+    memcpy(cur, nxt, sizeof cur);
+    ++steps;
+    if (outside_box_f32(cur, dims)) break;
+  }
+  float a1[3], a2[3], b1[3], b2[3];
+  dipole_step_f32(x0, N, x, mu, h, a1);
+  dipole_step_f32(a1, N, x, mu, h, a2);
+  dipole_step_f32(cur, N, x, mu, h, b1);
+  dipole_step_f32(b1, N, x, mu, h, b2);
+  float v1[3], v2[3], w1[3], w2[3];
+  for (int k = 0; k < 3; ++k) {
+    v1[k] = a1[k] - x0[k];
+    v2[k] = a2[k] - 2 * a1[k] + x0[k];
+    w1[k] = b1[k] - cur[k];
+    w2[k] = b2[k] - 2 * b1[k] + cur[k];
+  }
+  float cm = (curve_f32(v1, v2) + curve_f32(w1, w2)) / 2;
+  float s = 0.f;
+  for (int k = 0; k < 3; ++k) s += (float)pow(fabsf(x0[k] - cur[k]), 2);
+  ret[0] = (float)sqrt(s);
+  ret[1] = cm;
+  if (end) memcpy(end, cur, sizeof cur);
+  return steps;
+}

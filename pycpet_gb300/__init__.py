@@ -8,6 +8,7 @@ calculator hot-path methods (``drop_in``).
 """
 from ._lib import CpetgbError  # noqa: F401
 from .core import (GridBatch, TopoBatch, chi2_distance_matrix, esp_grid, field_distance_matrix,  # noqa: F401
-                   field_grid, point_field, synchronize, topo_hist2d, topo_hist2d_sets, topo_lines)
+                   field_grid, point_field, synchronize, topo_dipole_lines, topo_hist2d, topo_hist2d_sets,
+                   topo_lines)
 
 __version__ = "1.0.0"

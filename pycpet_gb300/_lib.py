@@ -43,12 +43,14 @@ SIGNATURES = {
     "cpetgb_calc_field": [_vp, _vp, _i, _vp, _vp],
     "cpetgb_thread_operation": [_i, _i, _f, _vp, _vp, _vp, _vp, _vp],
     "cpetgb_thread_operation_batch": [_i, _i, _vp, _f, _vp, _vp, _vp, _vp, _vp],
+    "cpetgb_thread_operation_dipole": [_i, _i, _f, _vp, _vp, _vp, _vp, _vp],
     "cpetgb_compute_esp_grid": [_i, _i, _vp, _vp, _vp, _vp],
     "cpetgb_field_grid": [_i, _i, _i, _i, _vp, _vp, _vp, _i, _vp, _vp],
     "cpetgb_esp_grid": [_i, _i, _i, _i, _vp, _vp, _vp, _vp, _vp],
     "cpetgb_grid_batch": [_i, _i, _i, _i, _i, _vp, _vp, _vp, _vp, _vp, _vp],
     "cpetgb_topo_lines": [_i, _i, _i, _i, _vp, _vp, _d, _vp, _vp, _vp, _vp, _vp, _vp, _vp],
     "cpetgb_topo_batch": [_i, _i, _i, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp],
+    "cpetgb_topo_dipole_lines": [_i, _i, _i, _i, _vp, _vp, _d, _vp, _vp, _vp, _vp, _vp, _vp, _vp],
     "cpetgb_tune_key": [_i, _i, _i, _d],
     "cpetgb_tune_variants": [_i],
     "cpetgb_tune_set": [_i, _i],

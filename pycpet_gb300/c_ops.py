@@ -50,6 +50,9 @@ class Math_ops:
         self._calc_field = L.cpetgb_calc_field
         self._calc_field.argtypes = [_f1, _f1, ctypes.c_int, _f2, _f1]
         self._calc_field.restype = ctypes.c_int
+        self._thread_op_dipole = L.cpetgb_thread_operation_dipole
+        self._thread_op_dipole.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_float, _f1, _f1, _f2, _f2, _f1]
+        self._thread_op_dipole.restype = ctypes.c_int
 
     def _with_precision(self, fn, *args):
         if self.precision is None:
@@ -86,6 +89,12 @@ class Math_ops:
         n_charges = len(Q)
         Q = Q.reshape(-1)
         self._with_precision(self._thread_op, n_charges, int(n_iter), step_size, x_0, dimensions, x, Q, res)
+        return res
+
+    def thread_operation_dipole(self, x_0, n_iter, x, mu, step_size, dimensions):
+        """One streamline through point dipoles (c_ops.py:304-325): res = (dist, curv)."""
+        res = np.zeros(2, dtype="float32")
+        self._with_precision(self._thread_op_dipole, len(mu), int(n_iter), step_size, x_0, dimensions, x, mu, res)
         return res
 
     def thread_operation_batch(self, x_0, n_iter, x, Q, step_size, dimensions):

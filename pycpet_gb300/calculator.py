@@ -12,6 +12,7 @@ Math wrappers (GPU):
   calculate_electric_field_c_shared_full_alt calculator.py:296-310  -> (3,) float32
   calculate_esp_c_shared_full                calculator.py:330-341  -> (1,) float32
   calculate_thread_c_shared                  calculator.py:344-348  -> (2,) float32
+  calculate_thread_c_shared_dipole           calculator.py:351-358  -> (2,) float32
 Streamline post-processing and histograms:
   curv / compute_curv_and_dist               calculator.py:501-561  (numpy, host)
   make_histograms                            calculator.py:596-718  (GPU binning, one launch)
@@ -122,6 +123,12 @@ def calculate_esp_c_shared_full(x_0, x, Q):
 def calculate_thread_c_shared(x_0, n_iter, x, Q, step_size, dimensions):
     return math_ops().thread_operation(x_0=x_0, n_iter=n_iter, x=x, Q=Q, step_size=step_size,
                                        dimensions=dimensions)
+
+
+def calculate_thread_c_shared_dipole(x_0, n_iter, x, mu, step_size, dimensions):
+    """One dipole streamline (CPET/utils/calculator.py:351-358)."""
+    return math_ops().thread_operation_dipole(x_0=x_0, n_iter=n_iter, x=x, mu=mu, step_size=step_size,
+                                              dimensions=dimensions)
 
 
 def compute_field_on_grid(grid_coords, x, Q):

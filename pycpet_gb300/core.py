@@ -206,12 +206,29 @@ def topo_lines(starts, n_iter, x, q, step, half_dims, precision="fp32c", return_
 
     Returns result (L,2) = [distance, mean curvature] in start order, and
     optionally the end points (L,3) and the Euler step counts (L,)."""
+    return _topo_lines(lib().cpetgb_topo_lines, 1, starts, n_iter, x, q, step, half_dims, precision, return_ends,
+                       return_steps)
+
+
+def topo_dipole_lines(starts, n_iter, x, mu, step, half_dims, precision="fp32c", return_ends=False,
+                      return_steps=False):
+    """thread_operation_dipole (CPET/utils/math_module.c:593-659) for every start
+    point: streamlines through the field of point dipoles at x (N,3) with
+    moments mu (N,3).  Outputs as topo_lines."""
+    return _topo_lines(lib().cpetgb_topo_dipole_lines, 3, starts, n_iter, x, mu, step, half_dims, precision,
+                       return_ends, return_steps)
+
+
+def _topo_lines(fn, src_tail, starts, n_iter, x, q, step, half_dims, precision, return_ends, return_steps):
     prec = precision_code(precision)
     half = np.ascontiguousarray(np.asarray(half_dims, dtype=np.float64).reshape(3))
     if _is_torch(starts):
         import torch
 
-        starts, x, q = _dev(starts, torch.float64, (3,)), _dev(x, torch.float64, (3,)), _dev(q, torch.float64)
+        starts, x = _dev(starts, torch.float64, (3,)), _dev(x, torch.float64, (3,))
+        q = _dev(q, torch.float64, (3,) if src_tail == 3 else ())
+        if q.shape[0] != x.shape[0]:
+            raise ValueError(f"{x.shape[0]} positions but {q.shape[0]} charges / moments")
         L = starts.shape[0]
         n_iter = _dev(n_iter if _is_torch(n_iter) else torch.as_tensor(np.broadcast_to(n_iter, (L,)).copy(),
                                                                        device=starts.device),
@@ -221,22 +238,26 @@ def topo_lines(starts, n_iter, x, q, step, half_dims, precision="fp32c", return_
         ends = torch.empty((L, 3), dtype=torch.float64, device=dev) if return_ends else None
         steps = torch.empty((L,), dtype=torch.int32, device=dev) if return_steps else None
         with torch.cuda.device(dev):
-            check(lib().cpetgb_topo_lines(prec, DEVICE, L, q.numel(), starts.data_ptr(), n_iter.data_ptr(),
-                                          float(step), half.ctypes.data, x.data_ptr(), q.data_ptr(),
-                                          res.data_ptr(), ends.data_ptr() if ends is not None else None,
-                                          steps.data_ptr() if steps is not None else None, _stream_of(starts)))
+            check(fn(prec, DEVICE, L, x.shape[0], starts.data_ptr(), n_iter.data_ptr(),
+                     float(step), half.ctypes.data, x.data_ptr(), q.data_ptr(),
+                     res.data_ptr(), ends.data_ptr() if ends is not None else None,
+                     steps.data_ptr() if steps is not None else None, _stream_of(starts)))
     else:
         starts = _host(starts, np.float64, (3,))
         L = starts.shape[0]
         n_iter = np.ascontiguousarray(np.broadcast_to(np.asarray(n_iter), (L,)), dtype=np.int32)
-        x, q = _host(x, np.float64, (3,)), _host(q, np.float64)
+        x, q = _host(x, np.float64, (3,)), _host(q, np.float64, (3,) if src_tail == 3 else None)
+        if src_tail == 1:
+            q = q.reshape(-1)
+        if len(q) != len(x):
+            raise ValueError(f"{len(x)} positions but {len(q)} charges / moments")
         res = np.empty((L, 2))
         ends = np.empty((L, 3)) if return_ends else None
         steps = np.empty(L, dtype=np.int32) if return_steps else None
-        check(lib().cpetgb_topo_lines(prec, HOST, L, q.size, starts.ctypes.data, n_iter.ctypes.data, float(step),
-                                      half.ctypes.data, x.ctypes.data, q.ctypes.data, res.ctypes.data,
-                                      ends.ctypes.data if ends is not None else None,
-                                      steps.ctypes.data if steps is not None else None, None))
+        check(fn(prec, HOST, L, len(x), starts.ctypes.data, n_iter.ctypes.data, float(step),
+                 half.ctypes.data, x.ctypes.data, q.ctypes.data, res.ctypes.data,
+                 ends.ctypes.data if ends is not None else None,
+                 steps.ctypes.data if steps is not None else None, None))
     out = [res]
     if return_ends:
         out.append(ends)

@@ -325,9 +325,10 @@ int grid_batch_impl(int kind, int prec, int mem, int clamp, int n_frames, const 
   return CPETGB_OK;
 }
 
+// source = kCharges: q[N] charges; kDipoles: q is mu[N][3], the dipole moments.
 int topo_impl(int prec, int mem, int L, int N, const double* starts, const int32_t* n_iter,
               double step, const double* half, const double* x, const double* q, double* result,
-              double* ends, int32_t* steps, void* stream) {
+              double* ends, int32_t* steps, void* stream, int source = kCharges) {
   if (!valid_prec(prec)) return fail(CPETGB_EINVAL, "bad precision %d", prec);
   if (!valid_mem(mem)) return fail(CPETGB_EINVAL, "bad memory kind %d", mem);
   if (L < 0 || N < 0) return fail(CPETGB_EINVAL, "negative line or charge count");
@@ -355,7 +356,8 @@ int topo_impl(int prec, int mem, int L, int N, const double* starts, const int32
     CK(h2d(const_cast<int32_t**>(&dn), S, n_iter, size_t(L)), "copy n_iter");
     if (N) {
       CK(h2d(const_cast<double**>(&dx), S, x, size_t(N) * 3), "copy charge positions");
-      CK(h2d(const_cast<double**>(&dq), S, q, size_t(N)), "copy charges");
+      CK(h2d(const_cast<double**>(&dq), S, q, size_t(N) * (source == kDipoles ? 3 : 1)),
+         "copy charges");
     }
     CK(S.get(&dres, size_t(L) * 2), "alloc result");
     if (ends) CK(S.get(&dends, size_t(L) * 3), "alloc ends");
@@ -365,13 +367,17 @@ int topo_impl(int prec, int mem, int L, int N, const double* starts, const int32
   const int64_t n_pad = ((std::max(N, 1) + int64_t(pad) - 1) / pad) * pad;
   unsigned char* packed = nullptr;
   int* queue = nullptr;
-  CK(S.get(&packed, size_t(n_pad) * packed_size(prec)), "alloc packed charges");
+  CK(S.get(&packed, size_t(n_pad) * topo_source_bytes(prec, source)), "alloc packed charges");
   CK(S.get(&queue, 1), "alloc queue");
   CK(cudaMemsetAsync(queue, 0, sizeof(int), s), "zero queue");
   if (reinterpret_cast<uintptr_t>(packed) % 16 != 0)
     return fail(CPETGB_ECUDA, "scratch allocation is not 16-byte aligned");
-  CK(launch_pack_topo(prec, N, n_pad, dx, dq, packed, s), "pack charges");
+  if (source == kDipoles)
+    CK(launch_pack_dipoles(prec, N, n_pad, dx, dq, packed, s), "pack dipoles");
+  else
+    CK(launch_pack_topo(prec, N, n_pad, dx, dq, packed, s), "pack charges");
   TopoParams p;
+  p.source = source;
   p.n_lines = L;
   p.n_charges = N;
   p.step = step;
@@ -915,6 +921,14 @@ int cpetgb_topo_lines(int precision, int mem, int n_lines, int n_charges, const 
                    result, ends, steps, stream);
 }
 
+int cpetgb_topo_dipole_lines(int precision, int mem, int n_lines, int n_dipoles,
+                             const double* starts, const int32_t* n_iter, double step,
+                             const double* half_dims, const double* x, const double* mu,
+                             double* result, double* ends, int32_t* steps, void* stream) {
+  return topo_impl(precision, mem, n_lines, n_dipoles, starts, n_iter, step, half_dims, x, mu,
+                   result, ends, steps, stream, kDipoles);
+}
+
 int cpetgb_topo_batch(int precision, int mem, int n_frames, const int64_t* desc,
                       const double* params, const double* starts, const int32_t* n_iter,
                       const double* x, const double* q, double* result, double* ends,
@@ -1090,6 +1104,27 @@ int cpetgb_thread_operation(int n_charges, int n_iter, float step_size, const fl
                             float* ret) {
   const int32_t it = n_iter;
   return cpetgb_thread_operation_batch(1, n_charges, &it, step_size, x_0, dimensions, x, Q, ret);
+}
+
+int cpetgb_thread_operation_dipole(int n_dipoles, int n_iter, float step_size, const float* x_0,
+                                   const float* dimensions, const float* x, const float* mu,
+                                   float* ret) {
+  if (n_dipoles < 0) return fail(CPETGB_EINVAL, "negative size");
+  if (!x_0 || !dimensions || !ret || (n_dipoles && (!x || !mu)))
+    return fail(CPETGB_EINVAL, "NULL pointer");
+  auto s = widen(x_0, 3);
+  auto xx = widen(x, size_t(n_dipoles) * 3);
+  auto mm = widen(mu, size_t(n_dipoles) * 3);
+  const double half[3] = {dimensions[0], dimensions[1], dimensions[2]};
+  const int32_t it = n_iter;
+  double res[2];
+  const int rc = cpetgb_topo_dipole_lines(g_default_prec.load(), CPETGB_HOST, 1, n_dipoles,
+                                          s.data(), &it, double(step_size), half, xx.data(),
+                                          mm.data(), res, nullptr, nullptr, nullptr);
+  if (rc != CPETGB_OK) return rc;
+  ret[0] = static_cast<float>(res[0]);
+  ret[1] = static_cast<float>(res[1]);
+  return CPETGB_OK;
 }
 
 }  // extern "C"

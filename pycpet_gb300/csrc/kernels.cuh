@@ -24,6 +24,13 @@ enum GridKind : int { kField = 0, kEsp = 1 };
 struct alignas(32) Charge64 {
   double x, y, z, q;
 };
+// Point dipole (FP64 streamline form): position and moment.
+struct alignas(16) Dipole64 {
+  double x, y, z, mx, my, mz;
+};
+static_assert(sizeof(Dipole64) == 48, "Dipole64 layout");
+// Sources of a streamline launch.
+enum Source : int { kCharges = 0, kDipoles = 1 };
 // FP32C uses float4 {x, y, z, q}.
 
 // One CTA of the grid kernel: a tile of up to kGridTilePts points of one frame
@@ -98,6 +105,7 @@ struct TopoParams {
   const TopoFrame* frames;   // device frame table (multi-frame launches) or null
   int n_frames;              // frames in the table
   int max_resident_pad;      // largest n_pad of a resident frame (shared-memory size)
+  int source = kCharges;     // kDipoles: packed holds dipoles (single-frame launches only)
 };
 // Single frame: p.frames == null, the frame is described by n_charges/step/half.
 cudaError_t launch_topo(int prec, const TopoParams& p, int num_sms, cudaStream_t s);
@@ -108,7 +116,13 @@ cudaError_t launch_topo_frames(int prec, const TopoParams& p, int num_sms, cudaS
 cudaError_t launch_pack_topo_frames(int prec, int n_frames, const TopoFrame* d_frames,
                                     const int64_t* d_src, const double* x, const double* q,
                                     void* packed, int max_pairs, cudaStream_t s);
-size_t topo_resident_limit(int prec);  // max charges held resident in shared memory
+// max sources (charges or dipoles) held resident in shared memory
+size_t topo_resident_limit(int prec, int source = kCharges);
+// bytes per packed source (FP32C charge 16, dipole 24; FP64 charge 32, dipole 48)
+size_t topo_source_bytes(int prec, int source);
+// Packs point dipoles x[n][3], mu[n][3] in the streamline layout (single frame).
+cudaError_t launch_pack_dipoles(int prec, int64_t n, int64_t n_pad, const double* x,
+                                const double* mu, void* packed, cudaStream_t s);
 int topo_charge_pad(int prec);         // packed charge arrays are padded to this multiple
 // Packs charges in the streamline kernel's layout (FP32C: pair layout; FP64: Charge64).
 cudaError_t launch_pack_topo(int prec, int64_t n, int64_t n_pad, const double* x, const double* q,

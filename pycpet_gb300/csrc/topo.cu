@@ -226,11 +226,48 @@ __device__ __forceinline__ void pair_run(const ulonglong2* __restrict__ A,
   }
 }
 
-template <int NA, int S>
+// Dipole pairs: A[p] = {x pair, y pair}, B[p] = {z pair, 3 mu_x pair},
+// C[p] = {mu_y pair, mu_z pair}.  Per dipole the term of
+// calc_field_base_dipole (CPET/utils/math_module.c:335-371) without the
+// constant factor (the step only uses the field's direction):
+//   r^-5 ((3 mu_x R_x + mu_y R_y + mu_z R_z) R_c - mu_c r^2)
+//   = w R_c - r^-3 mu_c,  w = (3 mu_x R_x + mu_y R_y + mu_z R_z) r^-5,
+// the x component taking mu_x as (3 mu_x) * (-1/3) r^-3.
+template <int NA, int S, int UNROLL>
+__device__ __forceinline__ void dipole_run(const ulonglong2* __restrict__ A,
+                                           const ulonglong2* __restrict__ B,
+                                           const ulonglong2* __restrict__ C, int base, int cnt,
+                                           const uint64_t (&ex2)[S][3], uint64_t (&part)[NA][3]) {
+  const uint64_t m_third = pk2(-1.f / 3.f, -1.f / 3.f), m_one = pk2(-1.f, -1.f);
+#pragma unroll UNROLL
+  for (int i = 0; i < cnt; ++i) {
+    const ulonglong2 a = A[base + 32 * i];  // {x pair, y pair}
+    const ulonglong2 b = B[base + 32 * i];  // {z pair, 3 mu_x pair}
+    const ulonglong2 c = C[base + 32 * i];  // {mu_y pair, mu_z pair}
+#pragma unroll
+    for (int e = 0; e < NA; ++e) {
+      const uint64_t dx = sub2(ex2[e][0], a.x);
+      const uint64_t dy = sub2(ex2[e][1], a.y);
+      const uint64_t dz = sub2(ex2[e][2], b.x);
+      const uint64_t r2 = fma2(dx, dx, fma2(dy, dy, mul2(dz, dz)));
+      const uint64_t ri = rsqrt2(r2);
+      const uint64_t ri2 = mul2(ri, ri);
+      const uint64_t ri3 = mul2(ri2, ri);
+      const uint64_t w = mul2(fma2(b.y, dx, fma2(c.x, dy, mul2(c.y, dz))), mul2(ri3, ri2));
+      const uint64_t t3 = mul2(ri3, m_third), tn = mul2(ri3, m_one);
+      part[e][0] = fma2(t3, b.y, fma2(w, dx, part[e][0]));
+      part[e][1] = fma2(tn, c.x, fma2(w, dy, part[e][1]));
+      part[e][2] = fma2(tn, c.y, fma2(w, dz, part[e][2]));
+    }
+  }
+}
+
+// C == nullptr: point charges (pair_run); otherwise point dipoles (dipole_run).
+template <int NA, int S, bool DIP = false>
 __device__ __forceinline__ void sweep_f32x2(const ulonglong2* __restrict__ A,
                                             const ulonglong2* __restrict__ B, int n_pairs,
                                             int lane, const uint64_t (&ex2)[S][3],
-                                            float& total) {
+                                            float& total, const ulonglong2* __restrict__ C = nullptr) {
   float acc[NA][3], cmp[NA][3];
 #pragma unroll
   for (int e = 0; e < NA; ++e)
@@ -247,10 +284,17 @@ __device__ __forceinline__ void sweep_f32x2(const ulonglong2* __restrict__ A,
     const int left = (n_pairs - base) >> 5;
     // about eight independent pair chains in flight per lane: unroll 8 / NA
     constexpr int kUnroll = NA >= 3 ? 2 : (NA == 2 ? 4 : 8);
-    if (left >= kLanePairs)
-      pair_run<NA, S, kUnroll>(A, B, base + lane, kLanePairs, ex2, part);
-    else
-      pair_run<NA, S, 1>(A, B, base + lane, left, ex2, part);
+    if constexpr (DIP) {
+      if (left >= kLanePairs)
+        dipole_run<NA, S, kUnroll>(A, B, C, base + lane, kLanePairs, ex2, part);
+      else
+        dipole_run<NA, S, 1>(A, B, C, base + lane, left, ex2, part);
+    } else {
+      if (left >= kLanePairs)
+        pair_run<NA, S, kUnroll>(A, B, base + lane, kLanePairs, ex2, part);
+      else
+        pair_run<NA, S, 1>(A, B, base + lane, left, ex2, part);
+    }
 #pragma unroll
     for (int e = 0; e < NA; ++e)
 #pragma unroll
@@ -335,6 +379,43 @@ __device__ __forceinline__ void sweep_f64(const Charge64* __restrict__ g, int n_
     }
 }
 
+// FP64 dipoles: Dipole64 records read from global memory (L2), padded with
+// zero moments far away.  Same term as dipole_run, in IEEE double.
+template <int NA, int S>
+__device__ __forceinline__ void sweep_dipole_f64(const Dipole64* __restrict__ g, int n_pad, int lane,
+                                                 const double (&ex)[S][3], double (&E)[S][3]) {
+  double acc[NA][3];
+#pragma unroll
+  for (int e = 0; e < NA; ++e)
+#pragma unroll
+    for (int c = 0; c < 3; ++c) acc[e][c] = 0.0;
+#pragma unroll 2
+  for (int j = lane; j < n_pad; j += 32) {
+    const Dipole64 d = g[j];
+#pragma unroll
+    for (int e = 0; e < NA; ++e) {
+      const double dx = __dsub_rn(ex[e][0], d.x);
+      const double dy = __dsub_rn(ex[e][1], d.y);
+      const double dz = __dsub_rn(ex[e][2], d.z);
+      const double r2 = __fma_rn(dx, dx, __fma_rn(dy, dy, __dmul_rn(dz, dz)));
+      const double r5 = __ddiv_rn(1.0, __dmul_rn(__dmul_rn(r2, r2), sqrt(r2)));
+      const double dot = __fma_rn(3.0 * d.mx, dx, __fma_rn(d.my, dy, __dmul_rn(d.mz, dz)));
+      acc[e][0] = __fma_rn(r5, __fma_rn(dot, dx, -__dmul_rn(d.mx, r2)), acc[e][0]);
+      acc[e][1] = __fma_rn(r5, __fma_rn(dot, dy, -__dmul_rn(d.my, r2)), acc[e][1]);
+      acc[e][2] = __fma_rn(r5, __fma_rn(dot, dz, -__dmul_rn(d.mz, r2)), acc[e][2]);
+    }
+  }
+#pragma unroll
+  for (int e = 0; e < NA; ++e)
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+      double v = acc[e][c];
+#pragma unroll
+      for (int off = 16; off >= 1; off >>= 1) v += __shfl_xor_sync(0xffffffffu, v, off);
+      E[e][c] = v;
+    }
+}
+
 // ---------------------------------------------------------------------------
 // Persistent kernel.
 // ---------------------------------------------------------------------------
@@ -342,10 +423,11 @@ __device__ __forceinline__ void sweep_f64(const Charge64* __restrict__ g, int n_
 // One line slot set per warp; processes the lines of frame `fc` (charge
 // arrays chA/chB in the FP32C pair layout, or g in Charge64) until the frame's
 // queue is exhausted and the warp's slots are drained.
-template <int PREC, int S>
+template <int PREC, int S, bool DIP>
 __device__ __forceinline__ void run_frame(const TopoParams& p, const FrameCtx& fc, int* queue,
                                           const ulonglong2* chA, const ulonglong2* chB,
-                                          const ulonglong2* smA, const ulonglong2* smB,
+                                          const ulonglong2* chC, const ulonglong2* smA,
+                                          const ulonglong2* smB, const ulonglong2* smC,
                                           bool resident, int n_pad, SlotRec* my_rec, int lane) {
   Slot sl;
   sl.line = -1;
@@ -388,17 +470,17 @@ __device__ __forceinline__ void run_frame(const TopoParams& p, const FrameCtx& f
       const int n_pairs = n_pad / 2;
       if (resident) {
         switch (na) {
-          case 1: sweep_f32x2<1, S>(smA, smB, n_pairs, lane, ex2, total); break;
-          case 2: sweep_f32x2<2, S>(smA, smB, n_pairs, lane, ex2, total); break;
-          case 3: sweep_f32x2<(S > 2 ? 3 : 2), S>(smA, smB, n_pairs, lane, ex2, total); break;
-          default: sweep_f32x2<S, S>(smA, smB, n_pairs, lane, ex2, total); break;
+          case 1: sweep_f32x2<1, S, DIP>(smA, smB, n_pairs, lane, ex2, total, smC); break;
+          case 2: sweep_f32x2<2, S, DIP>(smA, smB, n_pairs, lane, ex2, total, smC); break;
+          case 3: sweep_f32x2<(S > 2 ? 3 : 2), S, DIP>(smA, smB, n_pairs, lane, ex2, total, smC); break;
+          default: sweep_f32x2<S, S, DIP>(smA, smB, n_pairs, lane, ex2, total, smC); break;
         }
       } else {
         switch (na) {
-          case 1: sweep_f32x2<1, S>(chA, chB, n_pairs, lane, ex2, total); break;
-          case 2: sweep_f32x2<2, S>(chA, chB, n_pairs, lane, ex2, total); break;
-          case 3: sweep_f32x2<(S > 2 ? 3 : 2), S>(chA, chB, n_pairs, lane, ex2, total); break;
-          default: sweep_f32x2<S, S>(chA, chB, n_pairs, lane, ex2, total); break;
+          case 1: sweep_f32x2<1, S, DIP>(chA, chB, n_pairs, lane, ex2, total, chC); break;
+          case 2: sweep_f32x2<2, S, DIP>(chA, chB, n_pairs, lane, ex2, total, chC); break;
+          case 3: sweep_f32x2<(S > 2 ? 3 : 2), S, DIP>(chA, chB, n_pairs, lane, ex2, total, chC); break;
+          default: sweep_f32x2<S, S, DIP>(chA, chB, n_pairs, lane, ex2, total, chC); break;
         }
       }
       // component c of slot rank e sits in lanes (3e + c) << (5 - LV) and up
@@ -421,12 +503,22 @@ __device__ __forceinline__ void run_frame(const TopoParams& p, const FrameCtx& f
 #pragma unroll
         for (int c = 0; c < 3; ++c) ex[e][c] = __shfl_sync(0xffffffffu, sl.pos[c], src_of[e]);
       double Es[S][3];
-      const Charge64* g = reinterpret_cast<const Charge64*>(chA);
-      switch (na) {
-        case 1: sweep_f64<1, S>(g, n_pad, lane, ex, Es); break;
-        case 2: sweep_f64<2, S>(g, n_pad, lane, ex, Es); break;
-        case 3: sweep_f64<(S > 2 ? 3 : 2), S>(g, n_pad, lane, ex, Es); break;
-        default: sweep_f64<S, S>(g, n_pad, lane, ex, Es); break;
+      if constexpr (DIP) {
+        const Dipole64* g = reinterpret_cast<const Dipole64*>(chA);
+        switch (na) {
+          case 1: sweep_dipole_f64<1, S>(g, n_pad, lane, ex, Es); break;
+          case 2: sweep_dipole_f64<2, S>(g, n_pad, lane, ex, Es); break;
+          case 3: sweep_dipole_f64<(S > 2 ? 3 : 2), S>(g, n_pad, lane, ex, Es); break;
+          default: sweep_dipole_f64<S, S>(g, n_pad, lane, ex, Es); break;
+        }
+      } else {
+        const Charge64* g = reinterpret_cast<const Charge64*>(chA);
+        switch (na) {
+          case 1: sweep_f64<1, S>(g, n_pad, lane, ex, Es); break;
+          case 2: sweep_f64<2, S>(g, n_pad, lane, ex, Es); break;
+          case 3: sweep_f64<(S > 2 ? 3 : 2), S>(g, n_pad, lane, ex, Es); break;
+          default: sweep_f64<S, S>(g, n_pad, lane, ex, Es); break;
+        }
       }
       if (my_rank >= 0) {
         double E[3] = {0.0, 0.0, 0.0};
@@ -455,7 +547,9 @@ __device__ __forceinline__ void run_frame(const TopoParams& p, const FrameCtx& f
 // queue lasts, then moves on (after its own warps are done, so the shared
 // copy of the charges can be replaced).  Frames thus overlap only at their
 // tails and every frame switch costs a CTA one line's latency at most.
-template <int PREC, bool CAN_RESIDE, int S>
+// DIP: the sources are point dipoles (FP32C: three 16-byte pair blocks per
+// frame; FP64: Dipole64 records) instead of point charges.
+template <int PREC, bool CAN_RESIDE, int S, bool DIP>
 __global__ void __launch_bounds__(kTopoThreads, 1) topo_kernel(TopoParams p, TopoFrame frame0) {
   extern __shared__ __align__(128) unsigned char smem_raw[];
   __shared__ int s_skip;
@@ -483,7 +577,7 @@ __global__ void __launch_bounds__(kTopoThreads, 1) topo_kernel(TopoParams p, Top
     const bool resident = CAN_RESIDE && fr.resident;
     if (resident) {
       if (threadIdx.x == 0) {
-        const uint32_t total = static_cast<uint32_t>(fr.n_pad) * 16u;
+        const uint32_t total = static_cast<uint32_t>(fr.n_pad) * (DIP ? 24u : 16u);
         mbar_arrive_expect_tx(bar, total);
         const char* src = static_cast<const char*>(p.packed) + fr.packed_off * 16;
         constexpr uint32_t kChunk = 32768;
@@ -507,8 +601,10 @@ __global__ void __launch_bounds__(kTopoThreads, 1) topo_kernel(TopoParams p, Top
     const ulonglong2* gA = reinterpret_cast<const ulonglong2*>(
         static_cast<const char*>(p.packed) + fr.packed_off * elem);
     const ulonglong2* gB = gA + fr.n_pad / 2;
-    run_frame<PREC, S>(p, fc, queue, gA, gB, sm_ch, sm_ch + fr.n_pad / 2, resident, fr.n_pad, my_rec,
-                    lane);
+    const ulonglong2* gC = DIP ? gA + fr.n_pad : nullptr;
+    const ulonglong2* sC = DIP ? sm_ch + fr.n_pad : nullptr;
+    run_frame<PREC, S, DIP>(p, fc, queue, gA, gB, gC, sm_ch, sm_ch + fr.n_pad / 2, sC, resident,
+                            fr.n_pad, my_rec, lane);
   }
 }
 
@@ -798,26 +894,71 @@ __global__ void pack_pairs_kernel(int64_t n, int64_t n_pad, const double* __rest
   }
 }
 
-size_t topo_smem_bytes(int S, int max_resident_pad) {
-  return sizeof(SlotRec) * kTopoWarps * S + 128 + static_cast<size_t>(max_resident_pad) * 16;
+// Dynamic shared memory: slot records, the mbarrier, and the resident sources
+// (16 bytes per FP32C charge, 24 per FP32C dipole).
+// Dipoles, FP32C: A[p] = {x, x', y, y'}, B[p] = {z, z', 3 mu_x, 3 mu_x'},
+// C[p] = {mu_y, mu_y', mu_z, mu_z'} for the pair (2p, 2p + 1); padding =
+// zero moments far outside any box (they add exactly 0).
+__global__ void pack_dipole_pairs_kernel(int64_t n, int64_t n_pad, const double* __restrict__ x,
+                                         const double* __restrict__ mu, float4* __restrict__ out) {
+  const int64_t n_pairs = n_pad / 2;
+  for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < n_pairs;
+       p += (int64_t)gridDim.x * blockDim.x) {
+    float c[2][6];
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+      const int64_t i = 2 * p + h;
+      const bool in = i < n;
+      c[h][0] = in ? static_cast<float>(x[3 * i]) : 1.0e4f;
+      c[h][1] = in ? static_cast<float>(x[3 * i + 1]) : 1.0e4f;
+      c[h][2] = in ? static_cast<float>(x[3 * i + 2]) : 1.0e4f;
+      c[h][3] = in ? static_cast<float>(3.0 * mu[3 * i]) : 0.f;
+      c[h][4] = in ? static_cast<float>(mu[3 * i + 1]) : 0.f;
+      c[h][5] = in ? static_cast<float>(mu[3 * i + 2]) : 0.f;
+    }
+    out[p] = make_float4(c[0][0], c[1][0], c[0][1], c[1][1]);
+    out[n_pairs + p] = make_float4(c[0][2], c[1][2], c[0][3], c[1][3]);
+    out[2 * n_pairs + p] = make_float4(c[0][4], c[1][4], c[0][5], c[1][5]);
+  }
 }
 
-template <int PREC, bool CAN_RESIDE, int S>
+__global__ void pack_dipole64_kernel(int64_t n, int64_t n_pad, const double* __restrict__ x,
+                                     const double* __restrict__ mu, Dipole64* __restrict__ out) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n_pad;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    Dipole64 d;
+    if (i < n) {
+      d.x = x[3 * i]; d.y = x[3 * i + 1]; d.z = x[3 * i + 2];
+      d.mx = mu[3 * i]; d.my = mu[3 * i + 1]; d.mz = mu[3 * i + 2];
+    } else {
+      d.x = d.y = d.z = 1.0e4;
+      d.mx = d.my = d.mz = 0.0;
+    }
+    out[i] = d;
+  }
+}
+
+size_t topo_smem_bytes(int S, int max_resident_pad, bool dip = false) {
+  return sizeof(SlotRec) * kTopoWarps * S + 128 +
+         static_cast<size_t>(max_resident_pad) * (dip ? 24 : 16);
+}
+
+template <int PREC, bool CAN_RESIDE, int S, bool DIP>
 cudaError_t launch_topo_t(const TopoParams& p, const TopoFrame& f0, int total_lines, int num_sms,
                           cudaStream_t s) {
-  const size_t smem = topo_smem_bytes(S, CAN_RESIDE ? p.max_resident_pad : 0);
-  cudaError_t err = cudaFuncSetAttribute(topo_kernel<PREC, CAN_RESIDE, S>,
+  const size_t smem = topo_smem_bytes(S, CAN_RESIDE ? p.max_resident_pad : 0, DIP);
+  cudaError_t err = cudaFuncSetAttribute(topo_kernel<PREC, CAN_RESIDE, S, DIP>,
                                          cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          static_cast<int>(smem));
   if (err != cudaSuccess) return err;
   int per_sm = 1;
-  err = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, topo_kernel<PREC, CAN_RESIDE, S>,
+  err = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, topo_kernel<PREC, CAN_RESIDE, S, DIP>,
                                                       kTopoThreads, smem);
   if (err != cudaSuccess) return err;
   per_sm = std::max(per_sm, 1);
   const int max_useful = (total_lines + kTopoWarps * S - 1) / (kTopoWarps * S);
   const int grid = std::max(1, std::min(num_sms * per_sm, max_useful));
-  topo_kernel<PREC, CAN_RESIDE, S><<<grid, kTopoThreads, smem, s>>>(p, f0);
+  topo_kernel<PREC, CAN_RESIDE, S, DIP><<<grid, kTopoThreads, smem, s>>>(p, f0);
   return cudaGetLastError();
 }
 
@@ -896,15 +1037,33 @@ cudaError_t launch_engine(int prec, const EngineParams& e, int ctas, cudaStream_
   return cudaGetLastError();
 }
 
-size_t topo_resident_limit(int prec) {
-  if (prec != kFP32C) return 0;  // FP64 charges are read from global memory (L2)
+size_t topo_resident_limit(int prec, int source) {
+  if (prec != kFP32C) return 0;  // FP64 sources are read from global memory (L2)
   int dev = 0, optin = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
   const size_t fixed = topo_smem_bytes(4, 0) + 256;  // + static shared memory
   if (optin <= static_cast<int>(fixed)) return 0;
-  size_t n = (static_cast<size_t>(optin) - fixed) / 16;
+  size_t n = (static_cast<size_t>(optin) - fixed) / (source == kDipoles ? 24 : 16);
   return (n / kChargePad32) * kChargePad32;
+}
+
+cudaError_t launch_pack_dipoles(int prec, int64_t n, int64_t n_pad, const double* x,
+                                const double* mu, void* packed, cudaStream_t s) {
+  if (n_pad <= 0) return cudaSuccess;
+  if (prec == kFP32C) {
+    const int blocks = static_cast<int>(std::min<int64_t>((n_pad / 2 + 255) / 256, 4096));
+    pack_dipole_pairs_kernel<<<blocks, 256, 0, s>>>(n, n_pad, x, mu, static_cast<float4*>(packed));
+  } else {
+    const int blocks = static_cast<int>(std::min<int64_t>((n_pad + 255) / 256, 4096));
+    pack_dipole64_kernel<<<blocks, 256, 0, s>>>(n, n_pad, x, mu, static_cast<Dipole64*>(packed));
+  }
+  return cudaGetLastError();
+}
+
+size_t topo_source_bytes(int prec, int source) {
+  if (source == kDipoles) return prec == kFP32C ? 24 : sizeof(Dipole64);
+  return prec == kFP32C ? 16 : sizeof(Charge64);
 }
 
 cudaError_t launch_pack_topo(int prec, int64_t n, int64_t n_pad, const double* x, const double* q,
@@ -925,11 +1084,11 @@ cudaError_t launch_pack_topo_frames(int prec, int n_frames, const TopoFrame* d_f
   return cudaGetLastError();
 }
 
-template <int PREC, bool CAN_RESIDE>
+template <int PREC, bool CAN_RESIDE, bool DIP = false>
 cudaError_t launch_topo_s(const TopoParams& p, const TopoFrame& f0, int total_lines, int num_sms,
                           cudaStream_t s, int slots) {
-  return slots == 2 ? launch_topo_t<PREC, CAN_RESIDE, 2>(p, f0, total_lines, num_sms, s)
-                    : launch_topo_t<PREC, CAN_RESIDE, 4>(p, f0, total_lines, num_sms, s);
+  return slots == 2 ? launch_topo_t<PREC, CAN_RESIDE, 2, DIP>(p, f0, total_lines, num_sms, s)
+                    : launch_topo_t<PREC, CAN_RESIDE, 4, DIP>(p, f0, total_lines, num_sms, s);
 }
 
 // Single frame: p.packed holds round_up(n_charges, topo_charge_pad(prec)) charges
@@ -943,7 +1102,9 @@ cudaError_t launch_topo(int prec, const TopoParams& p_in, int num_sms, cudaStrea
   f0.line_off = 0;
   f0.n_pad = ((std::max(p.n_charges, 1) + pad - 1) / pad) * pad;
   f0.n_lines = p.n_lines;
-  f0.resident = (prec == kFP32C && static_cast<size_t>(f0.n_pad) <= topo_resident_limit(kFP32C));
+  const bool dip = p.source == kDipoles;
+  f0.resident = (prec == kFP32C &&
+                 static_cast<size_t>(f0.n_pad) <= topo_resident_limit(kFP32C, p.source));
   f0.pad_ = 0;
   f0.step = p.step;
   for (int k = 0; k < 3; ++k) f0.half[k] = p.half[k];
@@ -951,6 +1112,11 @@ cudaError_t launch_topo(int prec, const TopoParams& p_in, int num_sms, cudaStrea
   p.n_frames = 1;
   p.max_resident_pad = f0.resident ? f0.n_pad : 0;
   const int slots = tuned_topo_slots(prec, f0.resident, p.n_lines);
+  if (dip) {
+    if (prec == kFP64) return launch_topo_s<kFP64, false, true>(p, f0, p.n_lines, num_sms, s, slots);
+    if (f0.resident) return launch_topo_s<kFP32C, true, true>(p, f0, p.n_lines, num_sms, s, slots);
+    return launch_topo_s<kFP32C, false, true>(p, f0, p.n_lines, num_sms, s, slots);
+  }
   if (prec == kFP64) return launch_topo_s<kFP64, false>(p, f0, p.n_lines, num_sms, s, slots);
   if (f0.resident) return launch_topo_s<kFP32C, true>(p, f0, p.n_lines, num_sms, s, slots);
   return launch_topo_s<kFP32C, false>(p, f0, p.n_lines, num_sms, s, slots);

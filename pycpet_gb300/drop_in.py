@@ -1,6 +1,6 @@
 """Calculator-level drop-in for PyCPET's ``CPET.source.calculator.calculator``.
 
-The five hot-path methods the reference's dispatcher calls by name
+The hot-path methods the reference's dispatcher calls by name
 (CPET/source/CPET.py:105-108, 149, 186, 208) are provided as plain functions
 of ``self`` so they work both on ``Calculator`` below and, after
 ``patch_pycpet()``, on the reference class itself:
@@ -11,6 +11,8 @@ of ``self`` so they work both on ``Calculator`` below and, after
   compute_topo_complete_c_shared  calculator.py:675-712  -> (L,2) float32, start order
   compute_topo_GPU_batch_filter   calculator.py:793-978  -> (L,2) float32, start order
                                   (the reference returns finish order; same rows)
+  compute_topo_complete_c_shared_dipole  calculator.py:714-749  -> (L,2) float32
+                                  (point dipoles self.x / self.mu)
 
 Each reads ``self.x``, ``self.Q``, ``self.mesh``, ``self.random_start_points``,
 ``self.random_max_samples``, ``self.step_size`` and ``self.dimensions`` at call
@@ -27,12 +29,12 @@ import numpy as np
 
 from .calculator import (box_transformation, initialize_box_points_random, initialize_box_points_uniform,
                          volume_grid_counts)
-from .core import esp_grid, field_grid, topo_lines
+from .core import esp_grid, field_grid, topo_dipole_lines, topo_lines
 
 log = logging.getLogger(__name__)
 
 HOT_METHODS = ("compute_point_field", "compute_box", "compute_box_ESP", "compute_topo_complete_c_shared",
-               "compute_topo_GPU_batch_filter")
+               "compute_topo_GPU_batch_filter", "compute_topo_complete_c_shared_dipole")
 
 
 def _prec(self):
@@ -72,6 +74,18 @@ def compute_topo_complete_c_shared(self):
     return _topo(self)
 
 
+def compute_topo_complete_c_shared_dipole(self):
+    """Streamlines through point dipoles self.x / self.mu
+    (CPET/source/calculator.py:714-749; used by
+    CPET/source/scripts/field_topology_dipole.py:136-153)."""
+    starts = np.asarray(self.random_start_points, np.float64).reshape(-1, 3)
+    caps = np.asarray(self.random_max_samples).reshape(-1).astype(np.int32)
+    res = topo_dipole_lines(starts, caps, np.asarray(self.x, np.float64), np.asarray(self.mu, np.float64),
+                            float(self.step_size), np.asarray(self.dimensions, np.float64), precision=_prec(self))
+    self.hist = res.astype(np.float32)
+    return self.hist
+
+
 def compute_topo_GPU_batch_filter(self):
     return _topo(self)
 
@@ -106,6 +120,7 @@ class Calculator:
     compute_box_ESP = compute_box_ESP
     compute_topo_complete_c_shared = compute_topo_complete_c_shared
     compute_topo_GPU_batch_filter = compute_topo_GPU_batch_filter
+    compute_topo_complete_c_shared_dipole = compute_topo_complete_c_shared_dipole
 
     def __init__(self, options, x, Q):
         opts = dict(options)

@@ -21,6 +21,9 @@ Fixtures written (all small, compressed .npz):
   examples_topology.npz     the (distance, curvature) rows of example 3A's
                             shipped .top files and the reference's
                             make_histograms of them
+  ref_topo_dipole.npz       160 streamlines of 600 synthetic point dipoles
+                            through the reference's
+                            compute_topo_complete_c_shared_dipole
   ref_cluster.npz           ten synthetic .top files (900 rows each) through
                             the reference's make_histograms and
                             construct_distance_matrix, and eight synthetic
@@ -155,6 +158,30 @@ def ref_topo(scalc, out):
                         dims=dims, step=np.float32(step), result=np.asarray(hist, np.float32))
 
 
+def ref_topo_dipole(scalc, out):
+    from pycpet_gb300.synth import random_start_points
+
+    rng = np.random.default_rng(31)
+    x = rng.uniform(-12.0, 12.0, (900, 3))
+    x = x[np.linalg.norm(x, axis=1) > 2.5][:600].astype(np.float32)
+    mu = rng.normal(0.0, 0.3, (len(x), 3)).astype(np.float32)
+    dims = np.array([1.5, 1.5, 1.5], dtype=np.float32)
+    step = 0.01
+    starts = random_start_points(160, dims, seed=32).astype(np.float32)
+    caps = np.random.default_rng(33).integers(1, round(2 * np.linalg.norm(dims) / step), 160)
+    calc = scalc.calculator.__new__(scalc.calculator)
+    calc.x, calc.mu = x, mu
+    calc.random_start_points, calc.random_max_samples = starts, caps
+    calc.step_size, calc.dimensions, calc.n_samples = step, dims, len(starts)
+    calc.concur_slip = 4
+    calc.transformation_matrix = np.eye(3)
+    calc.center = np.zeros(3, np.float32)
+    calc.log = scalc.log
+    hist = calc.compute_topo_complete_c_shared_dipole()
+    np.savez_compressed(out, x=x, mu=mu, starts=starts, caps=caps.astype(np.int32), dims=dims,
+                        step=np.float32(step), result=np.asarray(hist, np.float32))
+
+
 def examples_topology(ref_root, ucalc, out):
     files = sorted(glob.glob(os.path.join(ref_root, "examples", "3A_field-topology", "outdir", "*.top")))
     rec = {}
@@ -197,6 +224,7 @@ def main():
     ref_topo(scalc, os.path.join(HERE, "ref_topo.npz"))
     examples_topology(a.ref, ucalc, os.path.join(HERE, "examples_topology.npz"))
     ref_cluster(ucalc, os.path.join(HERE, "ref_cluster.npz"))
+    ref_topo_dipole(scalc, os.path.join(HERE, "ref_topo_dipole.npz"))
     for f in sorted(glob.glob(os.path.join(HERE, "*.npz"))):
         print(f, os.path.getsize(f))
 

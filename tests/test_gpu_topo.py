@@ -197,7 +197,7 @@ def test_tuned_variants_agree(gpu_lib, oracle):
     pts = np.random.default_rng(1).uniform(-1, 1, (3000, 3))
     ref = oracle.field_grid_f64(pts, x, q)
     k = autotune.key(autotune.OP_GRID, "fp32c", _lib.FIELD, len(pts) * len(q))
-    for v in range(6):
+    for v in range(_lib.lib().cpetgb_tune_variants(autotune.OP_GRID)):
         autotune.set_variant(k, v)
         E = field_grid(pts, x, q, precision="fp32c")
         err = np.linalg.norm(E - ref, axis=1) / np.linalg.norm(ref, axis=1)

@@ -121,3 +121,31 @@ def test_cluster_oracle_matches_reference(golden, oracle):
         h = oracle.histogram2d(v[off[f]:off[f + 1], 0], v[off[f]:off[f + 1], 1], bins, rng)
         rows.append((h / np.sum(h)).flatten())
     np.testing.assert_array_equal(np.array(rows), c["hists"])
+
+
+def test_dipole_topology_matches_reference(golden, oracle):
+    """thread_operation_dipole through the reference's own
+    compute_topo_complete_c_shared_dipole (tests/golden/ref_topo_dipole.npz)."""
+    t = golden("ref_topo_dipole.npz")
+    R = t["result"]
+    r64, _, steps = oracle.topo_lines_dipole(t["starts"], t["caps"], t["x"], t["mu"], float(t["step"]), t["dims"])
+    assert np.abs(r64[:, 0] - R[:, 0]).max() < 5e-6
+    rel = np.abs(r64[:, 1] - R[:, 1]) / np.abs(R[:, 1])
+    assert np.median(rel) < 5e-3 and rel.max() < 5e-2
+    assert steps.min() >= 1 and np.all(steps <= t["caps"])
+    r32, _, _ = oracle.topo_lines_dipole(t["starts"], t["caps"], t["x"], t["mu"], t["step"], t["dims"], f32=True)
+    assert np.abs(r32[:, 0] - R[:, 0]).max() < 2e-6
+
+
+def test_dipole_semantics(oracle):
+    """A single dipole along +x at (10, 0, 0): on that axis R = (R_x, 0, 0), the
+    reference's term gives E_x = r^-5 (3 mu_x R_x^2 - mu_x r^2) = 2 mu_x / r^3 and
+    E_y = E_z = 0, so a line from the origin runs straight along +x and stops at
+    the first step strictly beyond 1.0."""
+    x = np.array([[10.0, 0.0, 0.0]])
+    mu = np.array([[1.0, 0.0, 0.0]])
+    res, ends, steps = oracle.topo_lines_dipole(np.zeros((1, 3)), [1000], x, mu, 0.1, [1.0, 1.0, 1.0])
+    assert steps[0] == 11
+    np.testing.assert_allclose(ends[0], [1.1, 0.0, 0.0], atol=1e-12)
+    np.testing.assert_allclose(res[0, 0], 1.1, atol=1e-12)
+    assert abs(res[0, 1]) < 1e-12
