@@ -180,7 +180,7 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-extras", action="store_true", help="skip the FP64 / grid / CPU comparison legs")
     ap.add_argument("--lines", type=int, default=N_LINES, help="streamlines per step (smaller cases for ncu)")
-    ap.add_argument("--workload", default="topo", choices=["topo", "grid", "topo-batch", "serve", "cluster"],
+    ap.add_argument("--workload", default="topo", choices=["topo", "grid", "topo-batch", "serve", "cluster", "topo-dipole"],
                     help="grid: the 64-frame batched volume + volume_ESP workload; topo-batch: "
                          "frames of 5,000-20,000 charges with uneven line counts in one launch")
     ap.add_argument("--requests", type=int, default=400, help="serve: number of requests")
@@ -222,6 +222,8 @@ def main():
         return serve_main(args, rank, world, dev, torch, dist)
     if args.workload == "cluster":
         return cluster_main(args, rank, world, dev, torch, dist)
+    if args.workload == "topo-dipole":
+        return dipole_main(args, rank, world, dev, torch, dist)
     x, q, starts, caps = make_inputs(rank)
     if args.lines != N_LINES:
         starts, caps = starts[:args.lines], caps[:args.lines]
@@ -542,6 +544,81 @@ def cluster_main(args, rank, world, dev, torch, dist):
         out["cpu_baseline"] = {"value": 768 * 767 // 2 * 400 / (t1 - t0), "unit": "terms/s", "cores": threads,
                                "kind": "port", "field_terms_per_s": 128 * 127 // 2 * 9261 / (t2 - t1),
                                "sample": "first 768 histograms / first 128 fields, oracle C restatement (FP64)"}
+    if rank == 0:
+        print(json.dumps(out), flush=True)
+    if world > 1:
+        dist.destroy_process_group()
+
+
+DIPOLE_FLOPS = 29  # 3 sub, r^2 5, r^-2 r^-3 r^-5 3, dot 5, w 1, 2 x 3 fma 12
+
+
+def dipole_main(args, rank, world, dev, torch, dist):
+    """--workload topo-dipole: streamlines through 8,000 point dipoles
+    (thread_operation_dipole; positions as the charge frames, moments
+    ~ N(0, 0.3)), --lines seeded start points (default 20,000) in the
+    1.5 A box, step 0.001 A, cap 6,000, FP32C device-resident; FP64 and the
+    CPU restatement on samples of the same lines."""
+    from pycpet_gb300 import _lib, topo_dipole_lines
+    from pycpet_gb300.synth import make_dipole_frame, random_start_points
+
+    n_lines = args.lines if args.lines != N_LINES else 20000
+    fr = make_dipole_frame(8000, seed=11 + 1000 * rank)
+    starts = random_start_points(n_lines, [HALF] * 3, seed=12 + 1000 * rank)
+    caps = np.full(n_lines, CAP, np.int32)
+    d = [torch.from_numpy(a).to(dev) for a in (starts, caps, fr["x"], fr["mu"])]
+    flush = torch.empty(L2_FLUSH_BYTES, dtype=torch.uint8, device=dev)
+    res, steps = topo_dipole_lines(*d[:2], d[2], d[3], STEP, [HALF] * 3, precision="fp32c", return_steps=True)
+    torch.cuda.synchronize()
+    pe = pair_evals(steps.cpu().numpy(), 8000)
+    for _ in range(args.warmup):
+        topo_dipole_lines(*d[:2], d[2], d[3], STEP, [HALF] * 3, precision="fp32c")
+    ffma = _lib.measure_peak(0)
+    torch.cuda.synchronize()
+    ts = []
+    for k in range(args.steps):
+        flush.fill_(k & 0xFF)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        topo_dipole_lines(*d[:2], d[2], d[3], STEP, [HALF] * 3, precision="fp32c")
+        e1.record()
+        torch.cuda.synchronize()
+        ts.append(e0.elapsed_time(e1) * 1e-3)
+    t = statistics.median(ts)
+    sub = slice(0, 1024)
+    t0 = time.perf_counter()
+    r64, s64 = topo_dipole_lines(starts[sub], caps[sub], fr["x"], fr["mu"], STEP, [HALF] * 3, precision="fp64",
+                                 return_steps=True)
+    t64 = time.perf_counter() - t0
+    r32 = res.cpu().numpy()[sub]
+    out = {"metric": "dipole streamlines/s (thread_operation_dipole)", "value": n_lines / t, "unit": "streamlines/s",
+           "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": t * 1e3,
+           "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+           "data": "synthetic (seeded)",
+           "config": {"workload": f"8,000 point dipoles, {n_lines} lines, half-width 1.5 A, step 0.001 A, cap 6,000",
+                      "l2": "flushed between timed steps"},
+           "pair_evals_per_s": pe / t,
+           "roofline": {"bound": "fp32", "achieved": pe * DIPOLE_FLOPS / t / 1e12, "peak": ffma / 1e12,
+                        "unit": "TFLOP/s", "frac": pe * DIPOLE_FLOPS / t / ffma,
+                        "work": f"{DIPOLE_FLOPS} flop per dipole term (21 FP32-pipe operations + 1 MUFU)"},
+           "fp64_first_1024": {"streamlines_per_s": 1024 / t64,
+                               "pair_evals_per_s": pair_evals(s64, 8000) / t64},
+           "fp32c_vs_fp64_first_1024": {"dist_max_A": float(np.abs(r32[:, 0] - r64[:, 0]).max()),
+                                        "curv_rel_p50": float(np.median(np.abs(r32[:, 1] - r64[:, 1]) /
+                                                                        np.abs(r64[:, 1]))),
+                                        "step_count_mismatch_frac": float(np.mean(steps.cpu().numpy()[sub] != s64))}}
+    if rank == 0 and world == 1:
+        from oracle import oracle
+
+        threads = os.cpu_count() or 1
+        n_cpu = 4 * threads
+        t0 = time.perf_counter()
+        _, _, sc = oracle.topo_lines_dipole(starts[:n_cpu], caps[:n_cpu], fr["x"], fr["mu"], STEP, [HALF] * 3,
+                                            f32=True, threads=threads)
+        tc = time.perf_counter() - t0
+        out["cpu_baseline"] = {"value": n_cpu / tc, "unit": "streamlines/s", "cores": threads, "kind": "port",
+                               "pair_evals_per_s": pair_evals(sc, 8000) / tc,
+                               "sample": f"first {n_cpu} lines, the reference's float arithmetic restated"}
     if rank == 0:
         print(json.dumps(out), flush=True)
     if world > 1:

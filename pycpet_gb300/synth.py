@@ -82,3 +82,14 @@ def random_start_points(n_lines: int, half_widths, seed: int):
     rng = np.random.default_rng(seed)
     hw = np.asarray(half_widths, dtype=np.float64)
     return np.column_stack([rng.uniform(-hw[k], hw[k], n_lines) for k in range(3)])
+
+
+def make_dipole_frame(n_dipoles: int, seed: int, sigma: float = 0.3):
+    """Point dipoles for the dipole streamline path: positions as make_frame's
+    charges (density 0.04 / A^3, >= 1 A apart, none within 2 A of the centre,
+    box frame), moments with components ~ N(0, sigma) e*A.
+
+    Returns dict(x=(N,3) f64, mu=(N,3) f64, seed=seed)."""
+    fr = make_frame(n_dipoles, seed)
+    mu = np.random.default_rng(seed + 104729).normal(0.0, sigma, (n_dipoles, 3))
+    return {"x": fr["x"], "mu": mu, "seed": seed}
