@@ -222,6 +222,17 @@ int cpetgb_topo_lines_noalloc(int precision, int n_lines, int n_charges, const d
 int cpetgb_topo_hist2d(int mem, int n_lines, const double* result, int nb_dist, int nb_curv,
                        const double* range, uint64_t* counts, double* edges, void* stream);
 
+/* ---- output text --------------------------------------------------------- */
+/* The body of save_numpy_as_dat (CPET/utils/io.py:50-109): the rows of a
+ * float32 matrix values[n_rows][n_cols] as numpy.savetxt(fmt="%.3f") writes
+ * them (each value correctly rounded to 3 decimals, ties to even; single
+ * spaces between values; "\n" after each row), formatted on the GPU.  *length
+ * (HOST) receives the byte count; text (HOST or DEVICE per mem, not
+ * NUL-terminated) is written when non-NULL and capacity >= *length, else
+ * CPETGB_ERANGE.  Synchronous: waits for `stream` to read the length. */
+int cpetgb_format_fixed3(int mem, int64_t n_rows, int n_cols, const float* values, char* text,
+                         int64_t capacity, int64_t* length, void* stream);
+
 /* ---- clustering front end: histograms and distance matrices -------------- */
 /* Histograms of many (distance, curvature) sets with one binning, in one
  * launch; replaces the per-file np.histogram2d loop of make_histograms

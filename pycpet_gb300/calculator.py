@@ -16,6 +16,8 @@ Math wrappers (GPU):
 Streamline post-processing and histograms:
   curv / compute_curv_and_dist               calculator.py:501-561  (numpy, host)
   make_histograms                            calculator.py:596-718  (GPU binning, one launch)
+Output (GPU text formatting):
+  save_numpy_as_dat                          CPET/utils/io.py:50-109
 Clustering front end (GPU distance matrices):
   distance_numpy                             calculator.py:975-978  (numpy, per pair)
   construct_distance_matrix                  calculator.py:1003-1015
@@ -31,7 +33,7 @@ import numpy as np
 
 from . import _lib
 from .c_ops import Math_ops
-from .core import chi2_distance_matrix, field_distance_matrix, topo_hist2d_sets
+from .core import chi2_distance_matrix, field_distance_matrix, format_fixed3, topo_hist2d_sets
 
 log = logging.getLogger(__name__)
 
@@ -245,6 +247,37 @@ def construct_distance_matrix_volume(fields, precision=None):
     (CPET/utils/calculator.py:1042-1058), one GPU launch; zero diagonal."""
     return field_distance_matrix(np.stack([np.asarray(f, np.float64).reshape(-1, 3) for f in fields]),
                                  _precision(precision))
+
+
+def save_numpy_as_dat(meta_data, volume, name):
+    """Volume output file of CPET/utils/io.py:50-109: the same seven header
+    lines, then the rows of `volume` as numpy.savetxt(fmt="%.3f") writes them,
+    formatted on the GPU for float32 / float16 volumes (the arrays
+    compute_box and compute_box_ESP return); other dtypes go through
+    numpy.savetxt itself, as the reference does."""
+    dimensions = meta_data["dimensions"]
+    num_steps_list = meta_data["num_steps"]
+    trans_mat = meta_data["transformation_matrix"].transpose()
+    center = meta_data["center"]
+    header = "#Sample Density: {} {} {}; Volume: Box: {} {} {}\n".format(
+        num_steps_list[0], num_steps_list[1], num_steps_list[2], dimensions[0], dimensions[1], dimensions[2])
+    header += "#Frame 0\n"
+    header += "#Center: {} {} {}\n".format(center[0], center[1], center[2])
+    header += "#Basis Matrix:\n# {} {} {}\n# {} {} {}\n# {} {} {}\n".format(
+        trans_mat[0][0], trans_mat[0][1], trans_mat[0][2], trans_mat[1][0], trans_mat[1][1], trans_mat[1][2],
+        trans_mat[2][0], trans_mat[2][1], trans_mat[2][2])
+    volume = np.asarray(volume)
+    if volume.dtype in (np.float32, np.float16) and volume.ndim in (1, 2):
+        body = format_fixed3(volume)
+    else:
+        import io
+
+        sink = io.BytesIO()
+        np.savetxt(sink, volume, fmt="%.3f")
+        body = sink.getvalue()
+    with open(name, "wb") as fh:
+        fh.write(header.encode())
+        fh.write(body)
 
 
 def _precision(p):

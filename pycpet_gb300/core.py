@@ -489,3 +489,28 @@ def field_distance_matrix(fields, precision="fp32c"):
     if fields.ndim != 3 or fields.shape[2] != 3:
         raise ValueError("fields must be (n_fields, n_points, 3)")
     return _distance_matrix(lib().cpetgb_field_distance_matrix, fields, 3, precision)
+
+
+# ---------------------------------------------------------------------------
+# Output text
+# ---------------------------------------------------------------------------
+
+def format_fixed3(values) -> bytes:
+    """Rows of a float32 (or float16) matrix as numpy.savetxt(fmt="%.3f")
+    writes them, formatted on the GPU (cpetgb_format_fixed3): each value
+    correctly rounded to 3 decimals, single spaces, "\\n" after each row."""
+    import ctypes
+
+    v = np.asarray(values)
+    if v.dtype not in (np.float32, np.float16):
+        raise TypeError("format_fixed3 formats float32 / float16 values exactly; got " + str(v.dtype))
+    cols = int(np.prod(v.shape[1:])) if v.ndim > 1 else 1
+    v = np.ascontiguousarray(v.reshape(v.shape[0] if v.ndim else 1, cols), dtype=np.float32)
+    n, m = v.shape
+    if n == 0:
+        return b""
+    length = ctypes.c_int64(0)
+    check(lib().cpetgb_format_fixed3(HOST, n, m, v.ctypes.data, None, 0, ctypes.byref(length), None))
+    buf = ctypes.create_string_buffer(max(length.value, 1))
+    check(lib().cpetgb_format_fixed3(HOST, n, m, v.ctypes.data, buf, length.value, ctypes.byref(length), None))
+    return buf.raw[:length.value]

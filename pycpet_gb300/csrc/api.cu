@@ -617,6 +617,44 @@ int hist_sets_impl(int mem, int n_sets, const int64_t* offsets, const double* va
   return CPETGB_OK;
 }
 
+int format_fixed3_impl(int mem, int64_t n_rows, int n_cols, const float* values, char* text,
+                       int64_t capacity, int64_t* length, void* stream) {
+  if (!valid_mem(mem)) return fail(CPETGB_EINVAL, "bad memory kind %d", mem);
+  if (n_rows < 0 || n_cols < 1) return fail(CPETGB_EINVAL, "need n_rows >= 0 and n_cols >= 1");
+  if (!length) return fail(CPETGB_EINVAL, "length pointer is NULL");
+  if (n_rows > 0 && !values) return fail(CPETGB_EINVAL, "values pointer is NULL");
+  if (n_rows > (int64_t(1) << 40) / n_cols) return fail(CPETGB_EINVAL, "matrix too large");
+  int rc;
+  Ctx* c = context(&rc);
+  if (!c) return rc;
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  if (!s) s = c->stream;
+  Scratch S(s);
+  const float* dv = values;
+  if (mem == CPETGB_HOST && n_rows)
+    CK(h2d(const_cast<float**>(&dv), S, values, size_t(n_rows) * n_cols), "copy values");
+  int64_t* off = nullptr;
+  int64_t* scratch = nullptr;
+  CK(S.get(&off, size_t(n_rows) + 1), "alloc offsets");
+  CK(S.get(&scratch, size_t(fixed3_scan_scratch(n_rows + 1))), "alloc scan scratch");
+  CK(launch_fixed3_offsets(n_rows, n_cols, dv, off, scratch, s), "length pass");
+  int64_t total = 0;
+  CK(cudaMemcpyAsync(&total, off + n_rows, sizeof(int64_t), cudaMemcpyDeviceToHost, s), "read length");
+  CK(cudaStreamSynchronize(s), "stream synchronize");
+  *length = total;
+  if (!text) return CPETGB_OK;
+  if (capacity < total) return fail(CPETGB_ERANGE, "text buffer holds %lld bytes, %lld needed",
+                                    (long long)capacity, (long long)total);
+  char* dt = text;
+  if (mem == CPETGB_HOST) CK(S.get(&dt, size_t(std::max<int64_t>(total, 1))), "alloc text");
+  CK(launch_fixed3_write(n_rows, n_cols, dv, off, dt, s), "write pass");
+  if (mem == CPETGB_HOST) {
+    if (total) CK(cudaMemcpyAsync(text, dt, size_t(total), cudaMemcpyDeviceToHost, s), "copy text");
+    return finish(c, s);
+  }
+  return CPETGB_OK;
+}
+
 // kind 0: chi-square over histogram rows [n][feat]; kind 1: field rows [n][feat][3].
 int distance_impl(int kind, int prec, int mem, int n, int feat, const double* src, double* out,
                   void* stream) {
@@ -1002,6 +1040,11 @@ int cpetgb_plan_destroy(cpetgb_plan* plan) {
 int cpetgb_topo_hist2d(int mem, int n_lines, const double* result, int nb_dist, int nb_curv,
                        const double* range, uint64_t* counts, double* edges, void* stream) {
   return hist_impl(mem, n_lines, result, nb_dist, nb_curv, range, counts, edges, stream);
+}
+
+int cpetgb_format_fixed3(int mem, int64_t n_rows, int n_cols, const float* values, char* text,
+                         int64_t capacity, int64_t* length, void* stream) {
+  return format_fixed3_impl(mem, n_rows, n_cols, values, text, capacity, length, stream);
 }
 
 int cpetgb_topo_hist2d_sets(int mem, int n_sets, const int64_t* offsets, const double* values,

@@ -171,6 +171,13 @@ cudaError_t launch_hist2d_sets(int n_sets, const int64_t* d_off, int64_t max_set
 
 // distance.cu: kind 0 = chi-square over histogram rows [n][feat]; kind 1 =
 // summed Euclidean norms over field rows [n][feat][3]; out [n][n].
+// format.cu: "%.3f" text of a float32 matrix (numpy.savetxt layout).
+int64_t fixed3_scan_scratch(int64_t n);
+cudaError_t launch_fixed3_offsets(int64_t n_rows, int n_cols, const float* v, int64_t* offsets,
+                                  int64_t* scratch, cudaStream_t s);
+cudaError_t launch_fixed3_write(int64_t n_rows, int n_cols, const float* v, const int64_t* offsets,
+                                char* out, cudaStream_t s);
+
 // splits > 1 (distance_splits) needs partial scratch of splits * n * n doubles.
 int distance_splits(int n, int feat, int num_sms);
 cudaError_t launch_distance_matrix(int prec, int kind, int n, int feat, const double* src,

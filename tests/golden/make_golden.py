@@ -24,6 +24,9 @@ Fixtures written (all small, compressed .npz):
   ref_topo_dipole.npz       160 streamlines of 600 synthetic point dipoles
                             through the reference's
                             compute_topo_complete_c_shared_dipole
+  ref_dat.npz               the field and potential volumes of ref_grid.npz
+                            written by the reference's save_numpy_as_dat (the
+                            .dat files' bytes) with their meta data
   ref_cluster.npz           ten synthetic .top files (900 rows each) through
                             the reference's make_histograms and
                             construct_distance_matrix, and eight synthetic
@@ -191,6 +194,25 @@ def examples_topology(ref_root, ucalc, out):
     np.savez_compressed(out, **rec)
 
 
+def ref_dat(ref_root, out):
+    import tempfile
+
+    import CPET.utils.io as rio
+
+    g = np.load(os.path.join(HERE, "ref_grid.npz"))
+    T = np.array([[0.8, 0.6, 0.0], [-0.6, 0.8, 0.0], [0.0, 0.0, 1.0]], dtype=np.float32)
+    meta = {"dimensions": np.array([1.0, 1.0, 1.0], np.float32), "num_steps": [11, 11, 11],
+            "transformation_matrix": T, "center": np.array([1.25, -3.5, 0.125], np.float32)}
+    rec = {"T": T, "dimensions": meta["dimensions"], "center": meta["center"], "num_steps": np.array([11, 11, 11])}
+    with tempfile.TemporaryDirectory() as tmp:
+        for key, vol in (("field", g["field"]), ("esp", g["esp_half"])):
+            path = os.path.join(tmp, f"{key}.dat")
+            rio.save_numpy_as_dat(meta, vol, path)
+            with open(path, "rb") as fh:
+                rec[f"{key}_dat"] = np.frombuffer(fh.read(), dtype=np.uint8)
+    np.savez_compressed(out, **rec)
+
+
 def ref_cluster(ucalc, out):
     import tempfile
 
@@ -224,6 +246,7 @@ def main():
     ref_topo(scalc, os.path.join(HERE, "ref_topo.npz"))
     examples_topology(a.ref, ucalc, os.path.join(HERE, "examples_topology.npz"))
     ref_cluster(ucalc, os.path.join(HERE, "ref_cluster.npz"))
+    ref_dat(a.ref, os.path.join(HERE, "ref_dat.npz"))
     ref_topo_dipole(scalc, os.path.join(HERE, "ref_topo_dipole.npz"))
     for f in sorted(glob.glob(os.path.join(HERE, "*.npz"))):
         print(f, os.path.getsize(f))
