@@ -180,7 +180,7 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-extras", action="store_true", help="skip the FP64 / grid / CPU comparison legs")
     ap.add_argument("--lines", type=int, default=N_LINES, help="streamlines per step (smaller cases for ncu)")
-    ap.add_argument("--workload", default="topo", choices=["topo", "grid", "topo-batch", "serve", "cluster", "topo-dipole"],
+    ap.add_argument("--workload", default="topo", choices=["topo", "grid", "topo-batch", "serve", "cluster", "topo-dipole", "dat"],
                     help="grid: the 64-frame batched volume + volume_ESP workload; topo-batch: "
                          "frames of 5,000-20,000 charges with uneven line counts in one launch")
     ap.add_argument("--requests", type=int, default=400, help="serve: number of requests")
@@ -224,6 +224,8 @@ def main():
         return cluster_main(args, rank, world, dev, torch, dist)
     if args.workload == "topo-dipole":
         return dipole_main(args, rank, world, dev, torch, dist)
+    if args.workload == "dat":
+        return dat_main(args, rank, world, dev, torch, dist)
     x, q, starts, caps = make_inputs(rank)
     if args.lines != N_LINES:
         starts, caps = starts[:args.lines], caps[:args.lines]
@@ -544,6 +546,68 @@ def cluster_main(args, rank, world, dev, torch, dist):
         out["cpu_baseline"] = {"value": 768 * 767 // 2 * 400 / (t1 - t0), "unit": "terms/s", "cores": threads,
                                "kind": "port", "field_terms_per_s": 128 * 127 // 2 * 9261 / (t2 - t1),
                                "sample": "first 768 histograms / first 128 fields, oracle C restatement (FP64)"}
+    if rank == 0:
+        print(json.dumps(out), flush=True)
+    if world > 1:
+        dist.destroy_process_group()
+
+
+def dat_main(args, rank, world, dev, torch, dist):
+    """--workload dat: one 51^3-point volume of a 20,000-charge frame, end to
+    end as the reference's run_volume does it (CPET/source/CPET.py:129-170):
+    the field on the grid (compute_field_on_grid) and the .dat file
+    (save_numpy_as_dat, CPET/utils/io.py:50-109) with its body formatted on
+    the GPU; beside it numpy.savetxt of the same rows on the host, the
+    reference's writer."""
+    import io as _io
+
+    from pycpet_gb300 import calculator as calc
+    from pycpet_gb300.synth import make_frame
+
+    fr = make_frame(20000, seed=21 + rank)
+    g = np.linspace(-2.5, 2.5, 51)
+    mesh = np.stack(np.meshgrid(g, g, g, indexing="ij"), -1).astype(np.float32)
+    meta = {"dimensions": np.array([2.5] * 3, np.float32), "num_steps": [51, 51, 51],
+            "transformation_matrix": np.eye(3, dtype=np.float32), "center": np.zeros(3, np.float32)}
+    x32, q32 = fr["x"].astype(np.float32), fr["q"].astype(np.float32).reshape(-1, 1)
+    tmp = tempfile.mkdtemp()
+    path = os.path.join(tmp, "frame_efield.dat")
+
+    def step():
+        vol = calc.compute_field_on_grid(mesh, x32, q32)
+        calc.save_numpy_as_dat(meta, vol, path)
+        return vol
+
+    for _ in range(args.warmup):
+        vol = step()
+    ts, tf = [], []
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        vol = calc.compute_field_on_grid(mesh, x32, q32)
+        t1 = time.perf_counter()
+        calc.save_numpy_as_dat(meta, vol, path)
+        t2 = time.perf_counter()
+        ts.append(t2 - t0)
+        tf.append(t2 - t1)
+    sink = _io.BytesIO()
+    t0 = time.perf_counter()
+    np.savetxt(sink, vol, fmt="%.3f")
+    t_np = time.perf_counter() - t0
+    body = calc.format_fixed3(vol)
+    assert body == sink.getvalue(), "GPU text differs from numpy.savetxt"
+    rows = vol.shape[0]
+    t = statistics.median(ts)
+    out = {"metric": "volume frames/s end to end (field + .dat file)", "value": 1.0 / t, "unit": "frames/s",
+           "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": t * 1e3,
+           "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+           "data": "synthetic (seeded)",
+           "config": {"workload": "51^3 volume of a 20,000-charge frame: compute_field_on_grid + save_numpy_as_dat",
+                      "rows": rows, "bytes": len(body)},
+           "writer_ms": statistics.median(tf) * 1e3, "writer_rows_per_s": rows / statistics.median(tf),
+           "numpy_savetxt_ms": t_np * 1e3, "numpy_savetxt_rows_per_s": rows / t_np,
+           "writer_speedup_vs_numpy": t_np / statistics.median(tf), "bytes_identical": True,
+           "e2e": {"value": 1.0 / t, "unit": "frames/s", "h2d_bytes_per_step": int(mesh.nbytes + x32.nbytes + q32.nbytes),
+                   "d2h_bytes_per_step": int(vol.nbytes + len(body))}}
     if rank == 0:
         print(json.dumps(out), flush=True)
     if world > 1:

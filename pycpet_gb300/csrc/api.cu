@@ -680,7 +680,11 @@ int distance_impl(int kind, int prec, int mem, int n, int feat, const double* sr
   const int splits = distance_splits(n, feat, c->sms);
   double* partial = nullptr;
   if (splits > 1) CK(S.get(&partial, size_t(splits) * n * n), "alloc partial sums");
-  CK(launch_distance_matrix(prec, kind, n, feat, dsrc, dout, splits, partial, s), "distance launch");
+  unsigned char* f32_rows = nullptr;
+  if (prec != CPETGB_FP64 && feat > 0)
+    CK(S.get(&f32_rows, distance_f32_bytes(kind, n, feat)), "alloc float rows");
+  CK(launch_distance_matrix(prec, kind, n, feat, dsrc, dout, splits, partial, f32_rows, s),
+     "distance launch");
   if (mem == CPETGB_HOST) {
     CK(cudaMemcpyAsync(out, dout, size_t(n) * n * sizeof(double), cudaMemcpyDeviceToHost, s),
        "copy matrix");

@@ -129,7 +129,7 @@ __device__ __forceinline__ void load_feat(Feat<Real, NC>& f, const double* p, bo
 // diagonal); with several it writes its partial sums to part[z][n][n].
 template <typename Real, int KIND>
 __global__ void __launch_bounds__(kThreads)
-    distance_kernel(int n, int feat, int per, const double* __restrict__ src,
+    distance_kernel(int n, int feat, int per, const void* __restrict__ src_raw,
                     double* __restrict__ out, double* __restrict__ part_out) {
   constexpr int NC = KIND == 0 ? 1 : 3;  // components per feature
   constexpr int kChunk = chunk_of<Real, NC>();
@@ -150,8 +150,16 @@ __global__ void __launch_bounds__(kThreads)
     for (int e = tid; e < kTile * kChunk; e += kThreads) {
       const int k = e % kChunk, row = e / kChunk, kk = k0 + k;
       const bool in = kk < ke;
-      load_feat<Real, NC>(sA[k][row], src + (i0 + row) * row_len + int64_t(kk) * NC, in && i0 + row < n);
-      load_feat<Real, NC>(sB[k][row], src + (j0 + row) * row_len + int64_t(kk) * NC, in && j0 + row < n);
+      if constexpr (sizeof(Real) == 4) {  // FP32C: rows converted once to Feat<float, NC>
+        const F* src = static_cast<const F*>(src_raw);
+        const F zero{};
+        sA[k][row] = (in && i0 + row < n) ? src[int64_t(i0 + row) * feat + kk] : zero;
+        sB[k][row] = (in && j0 + row < n) ? src[int64_t(j0 + row) * feat + kk] : zero;
+      } else {
+        const double* src = static_cast<const double*>(src_raw);
+        load_feat<Real, NC>(sA[k][row], src + (i0 + row) * row_len + int64_t(kk) * NC, in && i0 + row < n);
+        load_feat<Real, NC>(sB[k][row], src + (j0 + row) * row_len + int64_t(kk) * NC, in && j0 + row < n);
+      }
     }
     __syncthreads();
     Real part[4][4];
@@ -202,6 +210,16 @@ __global__ void __launch_bounds__(kThreads)
     }
 }
 
+// FP32C staging source: every value rounded to float once (a field point
+// padded to 4 components), instead of in every CTA that stages the row.
+template <int NC>
+__global__ void to_f32_kernel(int64_t n_feat, const double* __restrict__ in,
+                              Feat<float, NC>* __restrict__ out) {
+  for (int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; i < n_feat;
+       i += int64_t(gridDim.x) * blockDim.x)
+    load_feat<float, NC>(out[i], in + i * NC, true);
+}
+
 // Sum of the feature splits in split order (deterministic); chi2 halved;
 // zero diagonal.
 __global__ void distance_reduce_kernel(int kind, int n, int splits, const double* __restrict__ part,
@@ -228,9 +246,24 @@ int distance_splits(int n, int feat, int num_sms) {
   return std::max(1, std::min(s, feat / 64));  // at least 64 features per split
 }
 
+size_t distance_f32_bytes(int kind, int n, int feat) {
+  return size_t(n) * size_t(feat) * (kind == 0 ? sizeof(float) : sizeof(Feat<float, 3>));
+}
+
 cudaError_t launch_distance_matrix(int prec, int kind, int n, int feat, const double* src,
-                                   double* out, int splits, double* partial, cudaStream_t s) {
+                                   double* out, int splits, double* partial, void* f32_rows,
+                                   cudaStream_t s) {
   if (n <= 0) return cudaSuccess;
+  if (prec != kFP64 && int64_t(n) * feat > 0) {
+    const int64_t nf = int64_t(n) * feat;
+    const int blocks = static_cast<int>(std::min<int64_t>((nf + 255) / 256, 8192));
+    if (kind == 0)
+      to_f32_kernel<1><<<blocks, 256, 0, s>>>(nf, src, static_cast<Feat<float, 1>*>(f32_rows));
+    else
+      to_f32_kernel<3><<<blocks, 256, 0, s>>>(nf, src, static_cast<Feat<float, 3>*>(f32_rows));
+    cudaError_t err = cudaGetLastError();
+    if (err != cudaSuccess) return err;
+  }
   const int nb = (n + kTile - 1) / kTile;
   if (splits < 1 || feat == 0) splits = 1;
   const int per = (feat + splits - 1) / splits;
@@ -243,9 +276,9 @@ cudaError_t launch_distance_matrix(int prec, int kind, int n, int feat, const do
       distance_kernel<double, 1><<<grid, kThreads, 0, s>>>(n, feat, per, src, out, pout);
   } else {
     if (kind == 0)
-      distance_kernel<float, 0><<<grid, kThreads, 0, s>>>(n, feat, per, src, out, pout);
+      distance_kernel<float, 0><<<grid, kThreads, 0, s>>>(n, feat, per, f32_rows, out, pout);
     else
-      distance_kernel<float, 1><<<grid, kThreads, 0, s>>>(n, feat, per, src, out, pout);
+      distance_kernel<float, 1><<<grid, kThreads, 0, s>>>(n, feat, per, f32_rows, out, pout);
   }
   cudaError_t err = cudaGetLastError();
   if (err != cudaSuccess || splits == 1) return err;

@@ -179,8 +179,11 @@ cudaError_t launch_fixed3_write(int64_t n_rows, int n_cols, const float* v, cons
                                 char* out, cudaStream_t s);
 
 // splits > 1 (distance_splits) needs partial scratch of splits * n * n doubles.
+// FP32C also needs f32_rows scratch of distance_f32_bytes(kind, n, feat) bytes.
 int distance_splits(int n, int feat, int num_sms);
+size_t distance_f32_bytes(int kind, int n, int feat);
 cudaError_t launch_distance_matrix(int prec, int kind, int n, int feat, const double* src,
-                                   double* out, int splits, double* partial, cudaStream_t s);
+                                   double* out, int splits, double* partial, void* f32_rows,
+                                   cudaStream_t s);
 
 }  // namespace cpetgb
