@@ -222,6 +222,26 @@ int cpetgb_topo_lines_noalloc(int precision, int n_lines, int n_charges, const d
 int cpetgb_topo_hist2d(int mem, int n_lines, const double* result, int nb_dist, int nb_curv,
                        const double* range, uint64_t* counts, double* edges, void* stream);
 
+/* ---- frame preparation ----------------------------------------------------- */
+/* The per-frame preparation of PyCPET's calculator for parsed charges
+ * (CPET/source/calculator.py:239-251, 341-371), on the device:
+ *   radius > 0: filter_radius_whole_residue (CPET/utils/io.py:283-338) -- keep
+ *     the residues (runs of consecutive atoms with equal resid and resnum, both
+ *     int32 codes) with any atom strictly within `radius` of `center`;
+ *   rotation x <- (x - center) @ inv_basis (row-major 3x3, HOST; NULL: x - center);
+ *   box_half != NULL: filter_in_box (io.py:422-475) -- drop atoms strictly
+ *     inside the box, tested on x - center after the rotation as the
+ *     reference's call does (calculator.py:349-358);
+ *   box_shift != NULL: x <- x - box_shift (calculator.py:369-371).
+ * Survivors are written in input order to x_out[.][3], q_out; *n_out (HOST)
+ * receives their count.  center, inv_basis, box_half, box_shift are HOST
+ * arrays.  Synchronous: waits for `stream` to read the count. */
+int cpetgb_prepare_frame(int mem, int n_atoms, const double* x, const double* q,
+                         const int32_t* resid, const int32_t* resnum, const double* center,
+                         const double* inv_basis, double radius, const double* box_half,
+                         const double* box_shift, double* x_out, double* q_out, int* n_out,
+                         void* stream);
+
 /* ---- output text --------------------------------------------------------- */
 /* The body of save_numpy_as_dat (CPET/utils/io.py:50-109): the rows of a
  * float32 matrix values[n_rows][n_cols] as numpy.savetxt(fmt="%.3f") writes

@@ -514,3 +514,65 @@ def format_fixed3(values) -> bytes:
     buf = ctypes.create_string_buffer(max(length.value, 1))
     check(lib().cpetgb_format_fixed3(HOST, n, m, v.ctypes.data, buf, length.value, ctypes.byref(length), None))
     return buf.raw[:length.value]
+
+
+# ---------------------------------------------------------------------------
+# Frame preparation
+# ---------------------------------------------------------------------------
+
+def residue_codes(resid, resnum):
+    """int32 codes for the residue radius filter: equal (resid, resnum) give
+    equal codes (resid names such as 'ALA' are mapped to integers)."""
+    resid = np.asarray(resid)
+    if resid.dtype.kind in "iu":
+        codes = resid.astype(np.int32)
+    else:
+        _, codes = np.unique(resid.astype(str), return_inverse=True)
+    return np.ascontiguousarray(codes, dtype=np.int32), np.ascontiguousarray(resnum, dtype=np.int32)
+
+
+def prepare_frame(x, q, center, inv_basis=None, radius=None, resid=None, resnum=None, box_half=None,
+                  box_shift=None):
+    """The calculator's per-frame preparation on the GPU (cpetgb_prepare_frame;
+    CPET/source/calculator.py:239-251, 341-371): optional residue radius
+    filter (io.py:283-338), rotation (x - center) @ inv_basis, optional box
+    filter (io.py:422-475, with the reference's second recentring), optional
+    box shift.  Returns (x_box (M,3), q (M,)) float64 of the kept atoms in
+    input order (torch tensors when x is one)."""
+    import ctypes
+
+    c = np.ascontiguousarray(np.asarray(center, np.float64).reshape(3))
+    inv = None if inv_basis is None else np.ascontiguousarray(np.asarray(inv_basis, np.float64).reshape(9))
+    half = None if box_half is None else np.ascontiguousarray(np.asarray(box_half, np.float64).reshape(3))
+    shift = None if box_shift is None else np.ascontiguousarray(np.asarray(box_shift, np.float64).reshape(3))
+    r = 0.0 if radius is None else float(radius)
+    n_out = ctypes.c_int(0)
+    ptr = lambda a: None if a is None else a.ctypes.data
+    if r > 0.0:
+        if resid is None or resnum is None:
+            raise ValueError("the residue radius filter needs resid and resnum")
+        rc_, rn_ = residue_codes(resid, resnum)
+    if _is_torch(x):
+        import torch
+
+        x, q = _dev(x, torch.float64, (3,)), _dev(q, torch.float64, ())
+        n = x.shape[0]
+        xo = torch.empty_like(x)
+        qo = torch.empty_like(q)
+        dr = dn = None
+        if r > 0.0:
+            dr, dn = torch.from_numpy(rc_).to(x.device), torch.from_numpy(rn_).to(x.device)
+        with torch.cuda.device(x.device):
+            check(lib().cpetgb_prepare_frame(DEVICE, n, x.data_ptr(), q.data_ptr(),
+                                             dr.data_ptr() if dr is not None else None,
+                                             dn.data_ptr() if dn is not None else None, ptr(c), ptr(inv), r,
+                                             ptr(half), ptr(shift), xo.data_ptr(), qo.data_ptr(),
+                                             ctypes.byref(n_out), _stream_of(x)))
+        return xo[:n_out.value], qo[:n_out.value]
+    x, q = _host(x, np.float64, (3,)), _host(q, np.float64).reshape(-1)
+    n = x.shape[0]
+    xo, qo = np.empty_like(x), np.empty_like(q)
+    check(lib().cpetgb_prepare_frame(HOST, n, x.ctypes.data, q.ctypes.data, ptr(rc_) if r > 0 else None,
+                                     ptr(rn_) if r > 0 else None, ptr(c), ptr(inv), r, ptr(half), ptr(shift),
+                                     xo.ctypes.data, qo.ctypes.data, ctypes.byref(n_out), None))
+    return xo[:n_out.value], qo[:n_out.value]

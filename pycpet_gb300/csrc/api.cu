@@ -617,6 +617,65 @@ int hist_sets_impl(int mem, int n_sets, const int64_t* offsets, const double* va
   return CPETGB_OK;
 }
 
+int prepare_frame_impl(int mem, int n, const double* x, const double* q, const int32_t* resid,
+                       const int32_t* resnum, const double* center, const double* inv,
+                       double radius, const double* half, const double* shift, double* x_out,
+                       double* q_out, int* n_out, void* stream) {
+  if (!valid_mem(mem)) return fail(CPETGB_EINVAL, "bad memory kind %d", mem);
+  if (n < 0) return fail(CPETGB_EINVAL, "negative atom count");
+  if (!center || !n_out) return fail(CPETGB_EINVAL, "center / n_out pointer is NULL");
+  if (!std::isfinite(radius)) return fail(CPETGB_EINVAL, "radius must be finite (<= 0: no filter)");
+  for (int k = 0; k < 3; ++k)
+    if (!std::isfinite(center[k]) || (half && !(half[k] >= 0.0)) || (shift && !std::isfinite(shift[k])))
+      return fail(CPETGB_EINVAL, "center, box half-widths and shift must be finite (half-widths >= 0)");
+  if (inv)
+    for (int k = 0; k < 9; ++k)
+      if (!std::isfinite(inv[k])) return fail(CPETGB_EINVAL, "inverse basis must be finite");
+  *n_out = 0;
+  if (n == 0) return CPETGB_OK;
+  if (!x || !q || !x_out || !q_out) return fail(CPETGB_EINVAL, "array pointer is NULL");
+  if (radius > 0.0 && (!resid || !resnum))
+    return fail(CPETGB_EINVAL, "the residue radius filter needs resid and resnum");
+  int rc;
+  Ctx* c = context(&rc);
+  if (!c) return rc;
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  if (!s) s = c->stream;
+  Scratch S(s);
+  const double *dx = x, *dq = q;
+  const int32_t *dr = resid, *dn = resnum;
+  double *dxo = x_out, *dqo = q_out;
+  if (mem == CPETGB_HOST) {
+    CK(h2d(const_cast<double**>(&dx), S, x, size_t(n) * 3), "copy positions");
+    CK(h2d(const_cast<double**>(&dq), S, q, size_t(n)), "copy charges");
+    if (radius > 0.0) {
+      CK(h2d(const_cast<int32_t**>(&dr), S, resid, size_t(n)), "copy resid");
+      CK(h2d(const_cast<int32_t**>(&dn), S, resnum, size_t(n)), "copy resnum");
+    }
+    CK(S.get(&dxo, size_t(n) * 3), "alloc positions");
+    CK(S.get(&dqo, size_t(n)), "alloc charges");
+  }
+  unsigned char* scratch = nullptr;
+  int64_t* dcount = nullptr;
+  CK(S.get(&scratch, prep_scratch_bytes(n)), "alloc scratch");
+  CK(S.get(&dcount, 1), "alloc count");
+  CK(launch_prepare_frame(n, dx, dq, dr, dn, center, inv, radius, half, shift, dxo, dqo, scratch,
+                          dcount, s),
+     "frame preparation");
+  int64_t count = 0;
+  CK(cudaMemcpyAsync(&count, dcount, sizeof(int64_t), cudaMemcpyDeviceToHost, s), "read count");
+  CK(cudaStreamSynchronize(s), "stream synchronize");
+  *n_out = static_cast<int>(count);
+  if (mem == CPETGB_HOST && count) {
+    CK(cudaMemcpyAsync(x_out, dxo, size_t(count) * 3 * sizeof(double), cudaMemcpyDeviceToHost, s),
+       "copy positions");
+    CK(cudaMemcpyAsync(q_out, dqo, size_t(count) * sizeof(double), cudaMemcpyDeviceToHost, s),
+       "copy charges");
+    return finish(c, s);
+  }
+  return CPETGB_OK;
+}
+
 int format_fixed3_impl(int mem, int64_t n_rows, int n_cols, const float* values, char* text,
                        int64_t capacity, int64_t* length, void* stream) {
   if (!valid_mem(mem)) return fail(CPETGB_EINVAL, "bad memory kind %d", mem);
@@ -1044,6 +1103,15 @@ int cpetgb_plan_destroy(cpetgb_plan* plan) {
 int cpetgb_topo_hist2d(int mem, int n_lines, const double* result, int nb_dist, int nb_curv,
                        const double* range, uint64_t* counts, double* edges, void* stream) {
   return hist_impl(mem, n_lines, result, nb_dist, nb_curv, range, counts, edges, stream);
+}
+
+int cpetgb_prepare_frame(int mem, int n_atoms, const double* x, const double* q,
+                         const int32_t* resid, const int32_t* resnum, const double* center,
+                         const double* inv_basis, double radius, const double* box_half,
+                         const double* box_shift, double* x_out, double* q_out, int* n_out,
+                         void* stream) {
+  return prepare_frame_impl(mem, n_atoms, x, q, resid, resnum, center, inv_basis, radius, box_half,
+                            box_shift, x_out, q_out, n_out, stream);
 }
 
 int cpetgb_format_fixed3(int mem, int64_t n_rows, int n_cols, const float* values, char* text,

@@ -182,23 +182,23 @@ __global__ void write_rows_kernel(int64_t n_rows, int n_cols, const float* __res
   }
 }
 
+}  // namespace
+
 // Exclusive scan of n int64 values in place (recursive over tile sums).
-// scratch holds at least scan_scratch(n) values.
-cudaError_t scan_exclusive(int64_t n, int64_t* x, int64_t* scratch, cudaStream_t s) {
+// scratch holds at least scan_scratch_i64(n) values.
+cudaError_t scan_exclusive_i64(int64_t n, int64_t* x, int64_t* scratch, cudaStream_t s) {
   if (n <= 0) return cudaSuccess;
   const int64_t tiles = (n + kScanTile - 1) / kScanTile;
   scan_tiles_kernel<<<static_cast<unsigned>(tiles), kScanThreads, 0, s>>>(n, x, scratch);
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess || tiles == 1) return e;
-  e = scan_exclusive(tiles, scratch, scratch + tiles, s);
+  e = scan_exclusive_i64(tiles, scratch, scratch + tiles, s);
   if (e != cudaSuccess) return e;
   add_tile_offsets_kernel<<<static_cast<unsigned>(tiles), 256, 0, s>>>(n, x, scratch);
   return cudaGetLastError();
 }
 
-}  // namespace
-
-int64_t fixed3_scan_scratch(int64_t n) {
+int64_t scan_scratch_i64(int64_t n) {
   int64_t total = 0;
   while (n > 1) {
     n = (n + kScanTile - 1) / kScanTile;
@@ -206,6 +206,8 @@ int64_t fixed3_scan_scratch(int64_t n) {
   }
   return total + 1;
 }
+
+int64_t fixed3_scan_scratch(int64_t n) { return scan_scratch_i64(n); }
 
 // offsets [n_rows + 1] and scan scratch (fixed3_scan_scratch) in device memory;
 // offsets[n_rows] receives the total length.
@@ -219,7 +221,7 @@ cudaError_t launch_fixed3_offsets(int64_t n_rows, int n_cols, const float* v, in
   // offsets[n_rows] = 0 joins the scan so it ends up as the total
   e = cudaMemsetAsync(offsets + n_rows, 0, sizeof(int64_t), s);
   if (e != cudaSuccess) return e;
-  return scan_exclusive(n_rows + 1, offsets, scratch, s);
+  return scan_exclusive_i64(n_rows + 1, offsets, scratch, s);
 }
 
 cudaError_t launch_fixed3_write(int64_t n_rows, int n_cols, const float* v, const int64_t* offsets,

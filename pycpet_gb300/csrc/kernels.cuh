@@ -171,6 +171,19 @@ cudaError_t launch_hist2d_sets(int n_sets, const int64_t* d_off, int64_t max_set
 
 // distance.cu: kind 0 = chi-square over histogram rows [n][feat]; kind 1 =
 // summed Euclidean norms over field rows [n][feat][3]; out [n][n].
+// prep.cu: residue radius filter, rotation, box filter, shift, compaction of one
+// frame (device pointers; center/inv/half/shift on the host, inv/half/shift may
+// be null); the survivor count lands in d_count (device int64).
+size_t prep_scratch_bytes(int n);
+cudaError_t launch_prepare_frame(int n, const double* x, const double* q, const int32_t* resid,
+                                 const int32_t* resnum, const double* center, const double* inv,
+                                 double radius, const double* half, const double* shift,
+                                 double* x_out, double* q_out, void* scratch, int64_t* d_count,
+                                 cudaStream_t s);
+
+// format.cu: in-place exclusive scan of int64 values (scratch: scan_scratch_i64(n)).
+int64_t scan_scratch_i64(int64_t n);
+cudaError_t scan_exclusive_i64(int64_t n, int64_t* x, int64_t* scratch, cudaStream_t s);
 // format.cu: "%.3f" text of a float32 matrix (numpy.savetxt layout).
 int64_t fixed3_scan_scratch(int64_t n);
 cudaError_t launch_fixed3_offsets(int64_t n_rows, int n_cols, const float* v, int64_t* offsets,

@@ -29,7 +29,7 @@ import numpy as np
 
 from .calculator import (box_transformation, initialize_box_points_random, initialize_box_points_uniform,
                          volume_grid_counts)
-from .core import esp_grid, field_grid, topo_dipole_lines, topo_lines
+from .core import esp_grid, field_grid, prepare_frame, topo_dipole_lines, topo_lines
 
 log = logging.getLogger(__name__)
 
@@ -109,10 +109,13 @@ class Calculator:
 
     ``options`` uses the reference keys (CPET_method, dimensions, step_size,
     n_samples, initializer, max_streamline_init, dtype, center / x / y given
-    as coordinates, box_shift) plus the additive ``precision``.  ``x`` and
-    ``Q`` are the charges in the input frame; they are rotated into the box
-    frame exactly as CPET/source/calculator.py:341-346 does.  Parsing and
-    atom-spec filtering of PDB files stay PyCPET's job.
+    as coordinates, box_shift, filter_radius, filter_in_box) plus the
+    additive ``precision``.  ``x`` and ``Q`` are the charges in the input
+    frame; ``resid`` / ``resnum`` (per atom) are needed for filter_radius.
+    The radius filter, the rotation into the box frame, the box filter and
+    the shift run on the GPU (prepare_frame) with the reference's rules
+    (CPET/source/calculator.py:239-251, 341-371).  Parsing and atom-spec
+    filtering of PDB files stay PyCPET's job.
     """
 
     compute_point_field = compute_point_field
@@ -122,7 +125,7 @@ class Calculator:
     compute_topo_GPU_batch_filter = compute_topo_GPU_batch_filter
     compute_topo_complete_c_shared_dipole = compute_topo_complete_c_shared_dipole
 
-    def __init__(self, options, x, Q):
+    def __init__(self, options, x, Q, resid=None, resnum=None):
         opts = dict(options)
         self.precision = opts.get("precision", "fp32c")
         self.step_size = opts.get("step_size")
@@ -165,12 +168,14 @@ class Calculator:
                 self.n_samples = len(self.random_start_points)
         elif has_axes:
             self.transformation_matrix = box_transformation(self.center, self.x_vec_pt, self.y_vec_pt)
-        if has_axes:
-            self.x = (x - self.center) @ np.linalg.inv(self.transformation_matrix)
-        else:
-            self.x = x - self.center
-        if list(self.box_shift) != [0, 0, 0]:
-            self.x = self.x - np.array(self.box_shift)
+        # residue radius filter, rotation, box filter and shift on the GPU
+        # (CPET/source/calculator.py:239-251, 341-371)
+        radius = float(opts["filter_radius"]) if "filter_radius" in opts else None
+        box = self.dimensions if bool(opts.get("filter_in_box", False)) else None
+        shift = self.box_shift if list(self.box_shift) != [0, 0, 0] else None
+        inv = np.linalg.inv(self.transformation_matrix) if has_axes else None
+        self.x, self.Q = prepare_frame(x, self.Q, self.center, inv_basis=inv, radius=radius, resid=resid,
+                                       resnum=resnum, box_half=box, box_shift=shift)
         if self.dtype == "float32":
             self.x = self.x.astype(np.float32)
             self.Q = self.Q.astype(np.float32)

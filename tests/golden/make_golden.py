@@ -27,6 +27,9 @@ Fixtures written (all small, compressed .npz):
   ref_dat.npz               the field and potential volumes of ref_grid.npz
                             written by the reference's save_numpy_as_dat (the
                             .dat files' bytes) with their meta data
+  ref_prep.npz              a 3,000-atom synthetic frame with residue ids
+                            through the reference's filter_radius_whole_residue,
+                            rotation, filter_in_box and box shift
   ref_cluster.npz           ten synthetic .top files (900 rows each) through
                             the reference's make_histograms and
                             construct_distance_matrix, and eight synthetic
@@ -213,6 +216,36 @@ def ref_dat(ref_root, out):
     np.savez_compressed(out, **rec)
 
 
+def ref_prep(ucalc, out):
+    import CPET.utils.io as rio
+
+    rng = np.random.default_rng(41)
+    n = 3000
+    x = rng.uniform(-20.0, 20.0, (n, 3)) + np.array([3.0, -1.0, 2.0])
+    q = rng.normal(0.0, 0.4, n)
+    sizes = rng.integers(5, 20, n)
+    resnum, names, i, r = [], [], 0, 0
+    while len(resnum) < n:  # runs of 5-19 atoms; some neighbouring residues share a number
+        k = int(sizes[r])
+        resnum += [r // 2 + 1] * k
+        names += [["ALA", "GLY", "HIS", "LYS"][r % 4]] * k
+        r += 1
+    resnum, names = np.array(resnum[:n]), np.array(names[:n])
+    ID = [(j + 1, "CA", names[j], int(resnum[j]), "A") for j in range(n)]
+    center = np.array([3.0, -1.0, 2.0])
+    xa, ya = x[10], x[20]
+    T = ucalc.initialize_box_points_uniform(center=center, x=xa, y=ya, N_cr=[4, 4, 4],
+                                            dimensions=[1.5, 1.5, 1.5], inclusive=True)[1]
+    dims = np.array([3.0, 2.5, 4.0])
+    shift = np.array([0.25, -0.5, 0.125])
+    xf, qf, idf = rio.filter_radius_whole_residue(x=x, Q=q, ID=ID, center=center, radius=10.0)
+    xr = (xf - center) @ np.linalg.inv(T)
+    xb, qb, idb = rio.filter_in_box(x=xr, Q=qf, ID=np.array(idf, dtype=object), center=center, dimensions=dims)
+    xs = xb - shift
+    np.savez_compressed(out, x=x, q=q, resid=names, resnum=resnum, center=center, T=T, radius=10.0,
+                        dims=dims, shift=shift, x_ref=xs, q_ref=qb, n_after_radius=len(qf))
+
+
 def ref_cluster(ucalc, out):
     import tempfile
 
@@ -247,6 +280,7 @@ def main():
     examples_topology(a.ref, ucalc, os.path.join(HERE, "examples_topology.npz"))
     ref_cluster(ucalc, os.path.join(HERE, "ref_cluster.npz"))
     ref_dat(a.ref, os.path.join(HERE, "ref_dat.npz"))
+    ref_prep(ucalc, os.path.join(HERE, "ref_prep.npz"))
     ref_topo_dipole(scalc, os.path.join(HERE, "ref_topo_dipole.npz"))
     for f in sorted(glob.glob(os.path.join(HERE, "*.npz"))):
         print(f, os.path.getsize(f))

@@ -104,21 +104,3 @@ def test_make_histograms_binning_rules(golden):
         h, _, _ = np.histogram2d(t[:, 0], t[:, 1], bins=list(bins), range=list(rng))
         hists.append((h / h.sum()).flatten())
     np.testing.assert_array_equal(np.array(hists), g["hist"])
-
-
-def test_drop_in_calculator_state():
-    from pycpet_gb300.drop_in import Calculator
-
-    rng = np.random.default_rng(1)
-    x = rng.uniform(-10, 10, (50, 3))
-    Q = rng.normal(size=50)
-    opts = {"CPET_method": "volume", "dimensions": [1.0, 1.0, 1.0], "step_size": 0.1,
-            "center": [0.5, 0.0, 0.0], "x": [1.5, 0.0, 0.0], "y": [0.5, 1.0, 0.0]}
-    c = Calculator(opts, x, Q)
-    assert c.mesh.shape == (21, 21, 21, 3)
-    np.testing.assert_allclose(c.x, (x - [0.5, 0, 0]).astype(np.float32), atol=1e-6)
-    opts.update({"CPET_method": "topo", "n_samples": 100, "max_streamline_init": "fixed_rand"})
-    c = Calculator(opts, x, Q)
-    assert c.n_samples == 125 and c.random_start_points.shape == (125, 3)      # 5^3 interior grid
-    assert c.max_steps == round(2 * np.sqrt(3) / 0.1)
-    assert c.random_max_samples.min() >= 1 and c.random_max_samples.max() < c.max_steps

@@ -149,3 +149,24 @@ def test_dipole_semantics(oracle):
     np.testing.assert_allclose(ends[0], [1.1, 0.0, 0.0], atol=1e-12)
     np.testing.assert_allclose(res[0, 0], 1.1, atol=1e-12)
     assert abs(res[0, 1]) < 1e-12
+
+
+def test_frame_preparation_fixture_consistent(golden):
+    """The reference's frame preparation (tests/golden/ref_prep.npz) restated
+    with numpy on the host: residue runs, radius rule, rotation, box rule with
+    the second recentring, shift.  Pins the rules the GPU kernels follow."""
+    d = golden("ref_prep.npz")
+    x, q, c = d["x"], d["q"], d["center"]
+    resid, resnum = d["resid"], d["resnum"]
+    start = np.ones(len(x), bool)
+    start[1:] = (resid[1:] != resid[:-1]) | (resnum[1:] != resnum[:-1])
+    run = np.cumsum(start) - 1
+    near = np.linalg.norm(x - c, axis=1) < float(d["radius"])
+    keep_run = np.zeros(run.max() + 1, bool)
+    keep_run[run[near]] = True
+    k1 = keep_run[run]
+    assert k1.sum() == int(d["n_after_radius"])
+    xr = (x[k1] - c) @ np.linalg.inv(d["T"])
+    inside = np.all((xr - c > -d["dims"]) & (xr - c < d["dims"]), axis=1)
+    np.testing.assert_allclose(xr[~inside] - d["shift"], d["x_ref"], rtol=0, atol=1e-12)
+    np.testing.assert_array_equal(q[k1][~inside], d["q_ref"])
