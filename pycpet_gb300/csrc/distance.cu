@@ -24,10 +24,11 @@
 //   FP64   every operation in IEEE double; the per-point norm is formed as
 //          numpy forms it, (dx*dx + dy*dy) + dz*dz then sqrt, with no fused
 //          multiply-add, so only the order of the final sum differs.
-//   FP32C  values rounded to FP32 as they are staged; chi2 terms use the MUFU
-//          reciprocal, field terms the MUFU reciprocal square root; each
-//          staged chunk is summed plainly and Kahan-added (Kahan 1965)
-//          into a running (sum, compensation) pair.
+//   FP32C  values rounded to FP32 once before the launch; chi2 terms use the
+//          MUFU reciprocal (two columns per packed f32x2 instruction), field
+//          terms the MUFU reciprocal square root; each staged chunk is summed
+//          plainly and Kahan-added (Kahan 1965) into a running (sum,
+//          compensation) pair.
 // The term of (i, j) equals the term of (j, i) bit for bit in both forms, so
 // a tile on the diagonal writes an exactly symmetric block.
 #include <algorithm>
@@ -47,6 +48,12 @@ constexpr int kThreads = 256;  // 16 x 16 threads, 4 x 4 entries each
 template <typename Real, int NC>
 constexpr int chunk_of() {
   return NC == 1 ? 32 : (sizeof(Real) == 4 ? 16 : 8);
+}
+
+__device__ __forceinline__ uint64_t add2(uint64_t a, uint64_t b) {
+  uint64_t d;
+  asm("add.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+  return d;
 }
 
 __device__ __forceinline__ float rcp_mufu(float x) {
@@ -168,6 +175,43 @@ __global__ void __launch_bounds__(kThreads)
 #pragma unroll
       for (int c = 0; c < 4; ++c) part[r][c] = Real(0);
     const int kn = min(kChunk, ke - k0);
+    if constexpr (KIND == 0 && sizeof(Real) == 4) {
+      // chi2 in packed pairs of columns: one f32x2 instruction for two terms
+      uint64_t p2[4][2];
+#pragma unroll
+      for (int r = 0; r < 4; ++r) p2[r][0] = p2[r][1] = 0ull;
+#pragma unroll 4
+      for (int k = 0; k < kn; ++k) {
+        float a[4];
+        uint64_t b2[2];
+#pragma unroll
+        for (int r = 0; r < 4; ++r) a[r] = reinterpret_cast<const float&>(sA[k][ty + 16 * r]);
+        b2[0] = pk2(reinterpret_cast<const float&>(sB[k][tx]), reinterpret_cast<const float&>(sB[k][tx + 16]));
+        b2[1] = pk2(reinterpret_cast<const float&>(sB[k][tx + 32]), reinterpret_cast<const float&>(sB[k][tx + 48]));
+#pragma unroll
+        for (int r = 0; r < 4; ++r) {
+          const uint64_t aa = pk2(a[r], a[r]);
+#pragma unroll
+          for (int h = 0; h < 2; ++h) {
+            const uint64_t s2 = add2(aa, b2[h]);
+            const uint64_t d2 = sub2(aa, b2[h]);
+            float s0, s1;
+            upk2(s2, s0, s1);
+            const uint64_t rr = pk2(s0 != 0.f ? rcp_mufu(s0) : 0.f, s1 != 0.f ? rcp_mufu(s1) : 0.f);
+            p2[r][h] = fma2(mul2(d2, d2), rr, p2[r][h]);
+          }
+        }
+      }
+#pragma unroll
+      for (int r = 0; r < 4; ++r)
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+          float lo, hi;
+          upk2(p2[r][h], lo, hi);
+          part[r][2 * h] = reinterpret_cast<Real&>(lo);
+          part[r][2 * h + 1] = reinterpret_cast<Real&>(hi);
+        }
+    } else {
 #pragma unroll 4
     for (int k = 0; k < kn; ++k) {
       F a[4], b[4];
@@ -186,6 +230,7 @@ __global__ void __launch_bounds__(kThreads)
           else
             part[r][c] = __fadd_rn(part[r][c], t);
         }
+    }
     }
 #pragma unroll
     for (int r = 0; r < 4; ++r)
