@@ -1,7 +1,7 @@
 /*
  * oracle.c -- CPU restatement of PyCPET's Coulomb hot path.
  *
- * TEST INFRASTRUCTURE ONLY.  This file is the checker for the CUDA library in
+ * TEST INFRASTRUCTURE ONLY.  This file is the test oracle of the CUDA library in
  * pycpet_gb300/csrc: only tests/, __graft_entry__.smoke() and the CPU-baseline
  * leg of bench.py load it.  Nothing in the product path links or calls it.
  *

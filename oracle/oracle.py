@@ -1,4 +1,4 @@
-"""CPU checker for the GB300 Coulomb library.  TEST INFRASTRUCTURE ONLY.
+"""CPU oracle of the GB300 Coulomb library.  TEST INFRASTRUCTURE ONLY.
 
 Only tests/, ``__graft_entry__.smoke()`` and the CPU-baseline leg of bench.py may
 import this module.  It loads ``liboracle.so`` (built from oracle.c and

@@ -1,7 +1,7 @@
 /*
  * oracle_cluster.c -- CPU restatement of PyCPET's clustering distance matrices.
  *
- * TEST INFRASTRUCTURE ONLY (the checker of pycpet_gb300/csrc/distance.cu):
+ * TEST INFRASTRUCTURE ONLY (the test oracle of pycpet_gb300/csrc/distance.cu):
  * only tests/ and the CPU-baseline leg of bench.py load it.
  *
  *   oracle_chi2_matrix_f64   construct_distance_matrix with the metric

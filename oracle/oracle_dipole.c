@@ -1,7 +1,7 @@
 /*
  * oracle_dipole.c -- CPU restatement of PyCPET's dipole streamline path.
  *
- * TEST INFRASTRUCTURE ONLY (the checker of the dipole form of
+ * TEST INFRASTRUCTURE ONLY (the test oracle of the dipole form of
  * pycpet_gb300/csrc/topo.cu): only tests/ and bench.py's CPU-baseline leg load it.
  *
  * thread_operation_dipole (CPET/utils/math_module.c:593-659) is

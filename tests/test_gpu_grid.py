@@ -4,7 +4,7 @@ oracle and the reference's own outputs.
 Tolerances (stated here, checked per point):
   FP64 form   |dE| <= 1e-11 * max|E_oracle| (same arithmetic, other summation order)
   FP32C form  |dE| / |E_oracle| <= 1e-5 at every point whose |E_oracle| is at
-              least 1e-3 of the frame's median (the benchmark spec's bound), and
+              least 1e-3 of the frame's median, and
               |dE| <= 1e-5 * median|E_oracle| everywhere
 """
 import numpy as np

@@ -1,4 +1,4 @@
-"""Pins the CPU oracle to the reference before it is trusted as a checker.
+"""Pins the CPU oracle to the reference before the GPU tests rely on it.
 
 Golden fixtures (tests/golden, made by make_golden.py from the reference's own
 code and its C library compiled from source):
