@@ -153,9 +153,10 @@ int cpetgb_topo_batch(int precision, int mem, int n_frames, const int64_t* desc,
  * pycpet_gb300.autotune times the candidates and fills the table. */
 int cpetgb_tune_key(int op, int precision, int cls, double size);
 int cpetgb_tune_variants(int op);
-/* Largest frame (charges) whose streamline charges are held in shared memory
- * for the whole launch on the current device (the tuner's class 1); 0 for FP64. */
-int cpetgb_topo_resident_limit(int precision);
+/* Largest frame whose streamline sources are held in shared memory for the
+ * whole launch on the current device (the tuner's class 1): point charges
+ * (dipoles = 0) or point dipoles (dipoles = 1); 0 for FP64. */
+int cpetgb_topo_resident_limit(int precision, int dipoles);
 int cpetgb_tune_set(int key, int variant);   /* variant -1 removes the entry */
 int cpetgb_tune_get(int key);                /* -1 when untuned */
 

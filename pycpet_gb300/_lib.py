@@ -55,7 +55,7 @@ SIGNATURES = {
     "cpetgb_tune_variants": [_i],
     "cpetgb_tune_set": [_i, _i],
     "cpetgb_tune_get": [_i],
-    "cpetgb_topo_resident_limit": [_i],
+    "cpetgb_topo_resident_limit": [_i, _i],
     "cpetgb_grid_plan_create": [_vp, _i, _i, _i, _i, _vp, _vp, _vp, _vp, _vp],
     "cpetgb_topo_plan_create": [_vp, _i, _i, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp],
     "cpetgb_plan_launch": [_vp, _vp],

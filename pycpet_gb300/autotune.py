@@ -129,7 +129,7 @@ def tune_topo(frames, precision="fp32c", reps=2, verbose=False):
     tb = TopoBatch(frames, precision=precision, device=True)
     from ._lib import FP32C
 
-    resident_limit = lib().cpetgb_topo_resident_limit(precision_code(precision))
+    resident_limit = lib().cpetgb_topo_resident_limit(precision_code(precision), 0)
     check(min(resident_limit, 0))
     pad = 64  # FP32C streamline frames are padded to a multiple of 64 charges
     n_max = max(len(np.asarray(fr["q"]).reshape(-1)) for fr in frames)

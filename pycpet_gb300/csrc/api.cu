@@ -1065,11 +1065,11 @@ int cpetgb_tune_variants(int op) {
   return fail(CPETGB_EINVAL, "bad operation %d", op);
 }
 
-int cpetgb_topo_resident_limit(int precision) {
+int cpetgb_topo_resident_limit(int precision, int dipoles) {
   if (!valid_prec(precision)) return fail(CPETGB_EINVAL, "bad precision %d", precision);
   int rc;
   if (!context(&rc)) return rc;
-  return static_cast<int>(topo_resident_limit(precision));
+  return static_cast<int>(topo_resident_limit(precision, dipoles ? kDipoles : kCharges));
 }
 
 int cpetgb_tune_set(int key, int variant) {

@@ -64,6 +64,41 @@ def test_argument_validation_before_device(built):
     assert L.cpetgb_topo_hist2d(0, 1, None, 0, 20, None, None, None, None) == _lib.EINVAL
 
 
+def test_argument_validation_new_entry_points(built):
+    """The clustering, writer, preparation and dipole entry points refuse bad
+    arguments with a status and a message, before any device work."""
+    import ctypes
+
+    import numpy as np
+    from pycpet_gb300 import _lib
+
+    L = _lib.lib()
+    h = np.zeros((2, 3))
+    out = np.zeros((2, 2))
+    assert L.cpetgb_chi2_distance_matrix(7, 0, 2, 3, h.ctypes.data, out.ctypes.data, None) == _lib.EINVAL
+    assert L.cpetgb_field_distance_matrix(1, 0, -1, 3, h.ctypes.data, out.ctypes.data, None) == _lib.EINVAL
+    assert L.cpetgb_chi2_distance_matrix(1, 0, 2, 3, None, out.ctypes.data, None) == _lib.EINVAL
+    off = np.array([0, 1], np.int64)
+    rng = np.array([0.0, 1.0, 0.0, 1.0])
+    vals = np.zeros((1, 2))
+    cnt = np.zeros(4, np.uint64)
+    assert L.cpetgb_topo_hist2d_sets(0, 1, off.ctypes.data, vals.ctypes.data, 0, 4, rng.ctypes.data,
+                                     cnt.ctypes.data, None, None) == _lib.EINVAL
+    bad = np.array([0.0, np.nan, 0.0, 1.0])
+    assert L.cpetgb_topo_hist2d_sets(0, 1, off.ctypes.data, vals.ctypes.data, 2, 2, bad.ctypes.data,
+                                     cnt.ctypes.data, None, None) == _lib.ERANGE
+    length = ctypes.c_int64(0)
+    v = np.zeros((2, 3), np.float32)
+    assert L.cpetgb_format_fixed3(0, 2, 0, v.ctypes.data, None, 0, ctypes.byref(length), None) == _lib.EINVAL
+    x, q, c = np.zeros((4, 3)), np.zeros(4), np.zeros(3)
+    n_out = ctypes.c_int(0)
+    assert L.cpetgb_prepare_frame(0, 4, x.ctypes.data, q.ctypes.data, None, None, c.ctypes.data, None, 2.0,
+                                  None, None, x.ctypes.data, q.ctypes.data, ctypes.byref(n_out), None) == _lib.EINVAL
+    assert "resid" in _lib.last_error()
+    assert L.cpetgb_topo_dipole_lines(5, 0, 1, 1, x.ctypes.data, None, 0.1, c.ctypes.data, x.ctypes.data,
+                                      x.ctypes.data, out.ctypes.data, None, None, None) == _lib.EINVAL
+
+
 def test_tuning_table_round_trip(built):
     """The autotuner table is host state: keys, bounds and removal."""
     from pycpet_gb300 import _lib
