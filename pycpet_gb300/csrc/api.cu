@@ -414,12 +414,11 @@ struct TopoTables {
 
 // Frame table of a streamline launch: padded sizes, packed offsets (FP32C
 // frames occupy n_pad float4 -- the pair block A then B --, FP64 frames n_pad
-// Charge64), which frames stay resident in shared memory.
+// Charge64), how many charges of each frame stay resident in shared memory.
 int build_topo_tables(int prec, int F, const int64_t* desc, const double* params, TopoTables& t) {
   if (!valid_prec(prec)) return fail(CPETGB_EINVAL, "bad precision %d", prec);
   if (F < 0 || (F > 0 && (!desc || !params))) return fail(CPETGB_EINVAL, "bad frame table");
   const int pad = topo_charge_pad(prec);
-  const size_t res_limit = prec == CPETGB_FP32C ? topo_resident_limit(prec) : 0;
   t.frames.assign(F, TopoFrame{});
   t.src.assign(2 * size_t(F), 0);
   for (int f = 0; f < F; ++f) {
@@ -437,11 +436,11 @@ int build_topo_tables(int prec, int F, const int64_t* desc, const double* params
     t.packed_elems += fr.n_pad;
     fr.line_off = lo;
     fr.n_lines = static_cast<int32_t>(L);
-    fr.resident = (prec == CPETGB_FP32C && static_cast<size_t>(fr.n_pad) <= res_limit) ? 1 : 0;
+    fr.resident = topo_resident_count(prec, kCharges, fr.n_pad);
     fr.pad_ = 0;
     fr.step = pr[0];
     for (int k = 0; k < 3; ++k) fr.half[k] = pr[1 + k];
-    if (fr.resident) t.max_res = std::max(t.max_res, int(fr.n_pad));
+    t.max_res = std::max(t.max_res, int(fr.resident));
     t.max_pairs = std::max(t.max_pairs, int(fr.n_pad));
     t.src[2 * f] = co;
     t.src[2 * f + 1] = n;

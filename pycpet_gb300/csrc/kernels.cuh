@@ -82,7 +82,7 @@ struct TopoFrame {
   int64_t line_off;    // first line of the frame in starts / n_iter / result
   int32_t n_pad;       // padded charge count (a multiple of topo_charge_pad(prec))
   int32_t n_lines;
-  int32_t resident;    // 1: the frame's charges are staged in shared memory
+  int32_t resident;    // charges staged in shared memory: n_pad, a prefix, or 0
   int32_t pad_;
   double step;
   double half[3];
@@ -104,7 +104,7 @@ struct TopoParams {
   int* status;
   const TopoFrame* frames;   // device frame table (multi-frame launches) or null
   int n_frames;              // frames in the table
-  int max_resident_pad;      // largest n_pad of a resident frame (shared-memory size)
+  int max_resident_pad;      // largest TopoFrame::resident of the launch (shared-memory size)
   int source = kCharges;     // kDipoles: packed holds dipoles (single-frame launches only)
 };
 // Single frame: p.frames == null, the frame is described by n_charges/step/half.
@@ -118,6 +118,9 @@ cudaError_t launch_pack_topo_frames(int prec, int n_frames, const TopoFrame* d_f
                                     void* packed, int max_pairs, cudaStream_t s);
 // max sources (charges or dipoles) held resident in shared memory
 size_t topo_resident_limit(int prec, int source = kCharges);
+// sources of a frame of n_pad held in shared memory: n_pad when it fits, else
+// a prefix of whole Kahan runs; 0 for FP64 (TopoFrame::resident)
+int topo_resident_count(int prec, int source, int n_pad);
 // bytes per packed source (FP32C charge 16, dipole 24; FP64 charge 32, dipole 48)
 size_t topo_source_bytes(int prec, int source);
 // Packs point dipoles x[n][3], mu[n][3] in the streamline layout (single frame).

@@ -262,12 +262,20 @@ __device__ __forceinline__ void dipole_run(const ulonglong2* __restrict__ A,
   }
 }
 
-// C == nullptr: point charges (pair_run); otherwise point dipoles (dipole_run).
+// Pairs [0, res_pairs) are read from (sA, sB, sC) -- the shared-memory copy of
+// a frame's first pairs -- and pairs [res_pairs, n_pairs) from (A, B, C) in
+// global memory (L2).  res_pairs is n_pairs (all resident), 0 (none) or a
+// multiple of the 32 x kLanePairs pairs of one Kahan run, so every run reads
+// one source and the sums are the same whichever part is resident.
+// DIP: point dipoles (dipole_run, C used); otherwise point charges (pair_run).
 template <int NA, int S, bool DIP = false>
-__device__ __forceinline__ void sweep_f32x2(const ulonglong2* __restrict__ A,
-                                            const ulonglong2* __restrict__ B, int n_pairs,
-                                            int lane, const uint64_t (&ex2)[S][3],
-                                            float& total, const ulonglong2* __restrict__ C = nullptr) {
+__device__ __forceinline__ void sweep_f32x2(const ulonglong2* __restrict__ sA,
+                                            const ulonglong2* __restrict__ sB,
+                                            const ulonglong2* __restrict__ sC, int res_pairs,
+                                            const ulonglong2* __restrict__ A,
+                                            const ulonglong2* __restrict__ B,
+                                            const ulonglong2* __restrict__ C, int n_pairs,
+                                            int lane, const uint64_t (&ex2)[S][3], float& total) {
   float acc[NA][3], cmp[NA][3];
 #pragma unroll
   for (int e = 0; e < NA; ++e)
@@ -284,16 +292,31 @@ __device__ __forceinline__ void sweep_f32x2(const ulonglong2* __restrict__ A,
     const int left = (n_pairs - base) >> 5;
     // about eight independent pair chains in flight per lane: unroll 8 / NA
     constexpr int kUnroll = NA >= 3 ? 2 : (NA == 2 ? 4 : 8);
-    if constexpr (DIP) {
-      if (left >= kLanePairs)
-        dipole_run<NA, S, kUnroll>(A, B, C, base + lane, kLanePairs, ex2, part);
-      else
-        dipole_run<NA, S, 1>(A, B, C, base + lane, left, ex2, part);
-    } else {
-      if (left >= kLanePairs)
-        pair_run<NA, S, kUnroll>(A, B, base + lane, kLanePairs, ex2, part);
-      else
-        pair_run<NA, S, 1>(A, B, base + lane, left, ex2, part);
+    const int cnt = left >= kLanePairs ? kLanePairs : left;
+    if (base < res_pairs) {  // shared-memory copy
+      if constexpr (DIP) {
+        if (cnt == kLanePairs)
+          dipole_run<NA, S, kUnroll>(sA, sB, sC, base + lane, kLanePairs, ex2, part);
+        else
+          dipole_run<NA, S, 1>(sA, sB, sC, base + lane, cnt, ex2, part);
+      } else {
+        if (cnt == kLanePairs)
+          pair_run<NA, S, kUnroll>(sA, sB, base + lane, kLanePairs, ex2, part);
+        else
+          pair_run<NA, S, 1>(sA, sB, base + lane, cnt, ex2, part);
+      }
+    } else {  // global memory
+      if constexpr (DIP) {
+        if (cnt == kLanePairs)
+          dipole_run<NA, S, kUnroll>(A, B, C, base + lane, kLanePairs, ex2, part);
+        else
+          dipole_run<NA, S, 1>(A, B, C, base + lane, cnt, ex2, part);
+      } else {
+        if (cnt == kLanePairs)
+          pair_run<NA, S, kUnroll>(A, B, base + lane, kLanePairs, ex2, part);
+        else
+          pair_run<NA, S, 1>(A, B, base + lane, cnt, ex2, part);
+      }
     }
 #pragma unroll
     for (int e = 0; e < NA; ++e)
@@ -428,7 +451,7 @@ __device__ __forceinline__ void run_frame(const TopoParams& p, const FrameCtx& f
                                           const ulonglong2* chA, const ulonglong2* chB,
                                           const ulonglong2* chC, const ulonglong2* smA,
                                           const ulonglong2* smB, const ulonglong2* smC,
-                                          bool resident, int n_pad, SlotRec* my_rec, int lane) {
+                                          int res_pairs, int n_pad, SlotRec* my_rec, int lane) {
   Slot sl;
   sl.line = -1;
   sl.phase = kMain;
@@ -468,20 +491,20 @@ __device__ __forceinline__ void run_frame(const TopoParams& p, const FrameCtx& f
         }
       float total;
       const int n_pairs = n_pad / 2;
-      if (resident) {
-        switch (na) {
-          case 1: sweep_f32x2<1, S, DIP>(smA, smB, n_pairs, lane, ex2, total, smC); break;
-          case 2: sweep_f32x2<2, S, DIP>(smA, smB, n_pairs, lane, ex2, total, smC); break;
-          case 3: sweep_f32x2<(S > 2 ? 3 : 2), S, DIP>(smA, smB, n_pairs, lane, ex2, total, smC); break;
-          default: sweep_f32x2<S, S, DIP>(smA, smB, n_pairs, lane, ex2, total, smC); break;
-        }
-      } else {
-        switch (na) {
-          case 1: sweep_f32x2<1, S, DIP>(chA, chB, n_pairs, lane, ex2, total, chC); break;
-          case 2: sweep_f32x2<2, S, DIP>(chA, chB, n_pairs, lane, ex2, total, chC); break;
-          case 3: sweep_f32x2<(S > 2 ? 3 : 2), S, DIP>(chA, chB, n_pairs, lane, ex2, total, chC); break;
-          default: sweep_f32x2<S, S, DIP>(chA, chB, n_pairs, lane, ex2, total, chC); break;
-        }
+      switch (na) {
+        case 1:
+          sweep_f32x2<1, S, DIP>(smA, smB, smC, res_pairs, chA, chB, chC, n_pairs, lane, ex2, total);
+          break;
+        case 2:
+          sweep_f32x2<2, S, DIP>(smA, smB, smC, res_pairs, chA, chB, chC, n_pairs, lane, ex2, total);
+          break;
+        case 3:
+          sweep_f32x2<(S > 2 ? 3 : 2), S, DIP>(smA, smB, smC, res_pairs, chA, chB, chC, n_pairs, lane,
+                                               ex2, total);
+          break;
+        default:
+          sweep_f32x2<S, S, DIP>(smA, smB, smC, res_pairs, chA, chB, chC, n_pairs, lane, ex2, total);
+          break;
       }
       // component c of slot rank e sits in lanes (3e + c) << (5 - LV) and up
       float Ef[3];
@@ -574,15 +597,22 @@ __global__ void __launch_bounds__(kTopoThreads, 1) topo_kernel(TopoParams p, Top
     if (threadIdx.x == 0) s_skip = (*reinterpret_cast<volatile int*>(queue) >= fr.n_lines) ? 1 : 0;
     __syncthreads();
     if (s_skip) continue;
-    const bool resident = CAN_RESIDE && fr.resident;
-    if (resident) {
+    // resident sources: the frame's first fr.resident charges (all of them, or
+    // a prefix of whole Kahan runs when the frame exceeds shared memory)
+    const int res = CAN_RESIDE ? fr.resident : 0;
+    if (res > 0) {
       if (threadIdx.x == 0) {
-        const uint32_t total = static_cast<uint32_t>(fr.n_pad) * (DIP ? 24u : 16u);
-        mbar_arrive_expect_tx(bar, total);
+        const uint32_t blk = static_cast<uint32_t>(res / 2) * 16u;  // bytes of one block's prefix
+        const int n_blk = DIP ? 3 : 2;
+        mbar_arrive_expect_tx(bar, blk * n_blk);
         const char* src = static_cast<const char*>(p.packed) + fr.packed_off * 16;
         constexpr uint32_t kChunk = 32768;
-        for (uint32_t off = 0; off < total; off += kChunk)
-          bulk_g2s(reinterpret_cast<char*>(sm_ch) + off, src + off, min(kChunk, total - off), bar);
+        for (int b = 0; b < n_blk; ++b) {  // block b of the frame starts at b * n_pad/2 pairs
+          const char* bs = src + static_cast<size_t>(b) * (fr.n_pad / 2) * 16;
+          char* bd = reinterpret_cast<char*>(sm_ch) + static_cast<size_t>(b) * blk;
+          for (uint32_t off = 0; off < blk; off += kChunk)
+            bulk_g2s(bd + off, bs + off, min(kChunk, blk - off), bar);
+        }
       }
       const bool mine = mbar_wait(bar, load_parity, p.status);
       load_parity ^= 1u;
@@ -602,9 +632,9 @@ __global__ void __launch_bounds__(kTopoThreads, 1) topo_kernel(TopoParams p, Top
         static_cast<const char*>(p.packed) + fr.packed_off * elem);
     const ulonglong2* gB = gA + fr.n_pad / 2;
     const ulonglong2* gC = DIP ? gA + fr.n_pad : nullptr;
-    const ulonglong2* sC = DIP ? sm_ch + fr.n_pad : nullptr;
-    run_frame<PREC, S, DIP>(p, fc, queue, gA, gB, gC, sm_ch, sm_ch + fr.n_pad / 2, sC, resident,
-                            fr.n_pad, my_rec, lane);
+    const ulonglong2* sC = DIP ? sm_ch + res : nullptr;
+    run_frame<PREC, S, DIP>(p, fc, queue, gA, gB, gC, sm_ch, sm_ch + res / 2, sC, res / 2, fr.n_pad,
+                            my_rec, lane);
   }
 }
 
@@ -805,10 +835,10 @@ __global__ void __launch_bounds__(kEngineThreads, 2) engine_kernel(EngineParams 
         float total;
         const int n_pairs = n_pad / 2;
         switch (na) {
-          case 1: sweep_f32x2<1, S>(gA, gB, n_pairs, lane, ex2, total); break;
-          case 2: sweep_f32x2<2, S>(gA, gB, n_pairs, lane, ex2, total); break;
-          case 3: sweep_f32x2<(S > 2 ? 3 : 2), S>(gA, gB, n_pairs, lane, ex2, total); break;
-          default: sweep_f32x2<S, S>(gA, gB, n_pairs, lane, ex2, total); break;
+          case 1: sweep_f32x2<1, S>(gA, gB, nullptr, 0, gA, gB, nullptr, n_pairs, lane, ex2, total); break;
+          case 2: sweep_f32x2<2, S>(gA, gB, nullptr, 0, gA, gB, nullptr, n_pairs, lane, ex2, total); break;
+          case 3: sweep_f32x2<(S > 2 ? 3 : 2), S>(gA, gB, nullptr, 0, gA, gB, nullptr, n_pairs, lane, ex2, total); break;
+          default: sweep_f32x2<S, S>(gA, gB, nullptr, 0, gA, gB, nullptr, n_pairs, lane, ex2, total); break;
         }
         float Ef[3];
         const int rk = my_rank >= 0 ? my_rank : 0;
@@ -1037,6 +1067,17 @@ cudaError_t launch_engine(int prec, const EngineParams& e, int ctas, cudaStream_
   return cudaGetLastError();
 }
 
+// Charges (or dipoles) of a frame held in shared memory: all of them when the
+// frame fits, else the largest prefix of whole Kahan runs (32 x kLanePairs
+// pairs) that fits; 0 for FP64.
+int topo_resident_count(int prec, int source, int n_pad) {
+  const int limit = static_cast<int>(topo_resident_limit(prec, source));
+  if (limit <= 0) return 0;
+  if (n_pad <= limit) return n_pad;
+  constexpr int kRun = 2 * 32 * kLanePairs;
+  return (limit / kRun) * kRun;
+}
+
 size_t topo_resident_limit(int prec, int source) {
   if (prec != kFP32C) return 0;  // FP64 sources are read from global memory (L2)
   int dev = 0, optin = 0;
@@ -1103,22 +1144,21 @@ cudaError_t launch_topo(int prec, const TopoParams& p_in, int num_sms, cudaStrea
   f0.n_pad = ((std::max(p.n_charges, 1) + pad - 1) / pad) * pad;
   f0.n_lines = p.n_lines;
   const bool dip = p.source == kDipoles;
-  f0.resident = (prec == kFP32C &&
-                 static_cast<size_t>(f0.n_pad) <= topo_resident_limit(kFP32C, p.source));
+  f0.resident = topo_resident_count(prec, p.source, f0.n_pad);
   f0.pad_ = 0;
   f0.step = p.step;
   for (int k = 0; k < 3; ++k) f0.half[k] = p.half[k];
   p.frames = nullptr;
   p.n_frames = 1;
-  p.max_resident_pad = f0.resident ? f0.n_pad : 0;
-  const int slots = tuned_topo_slots(prec, f0.resident, p.n_lines);
+  p.max_resident_pad = f0.resident;
+  const int slots = tuned_topo_slots(prec, f0.resident == f0.n_pad, p.n_lines);
   if (dip) {
     if (prec == kFP64) return launch_topo_s<kFP64, false, true>(p, f0, p.n_lines, num_sms, s, slots);
-    if (f0.resident) return launch_topo_s<kFP32C, true, true>(p, f0, p.n_lines, num_sms, s, slots);
+    if (f0.resident > 0) return launch_topo_s<kFP32C, true, true>(p, f0, p.n_lines, num_sms, s, slots);
     return launch_topo_s<kFP32C, false, true>(p, f0, p.n_lines, num_sms, s, slots);
   }
   if (prec == kFP64) return launch_topo_s<kFP64, false>(p, f0, p.n_lines, num_sms, s, slots);
-  if (f0.resident) return launch_topo_s<kFP32C, true>(p, f0, p.n_lines, num_sms, s, slots);
+  if (f0.resident > 0) return launch_topo_s<kFP32C, true>(p, f0, p.n_lines, num_sms, s, slots);
   return launch_topo_s<kFP32C, false>(p, f0, p.n_lines, num_sms, s, slots);
 }
 
