@@ -410,6 +410,7 @@ struct TopoTables {
   std::vector<int64_t> src;  // per frame {charge offset, charge count} into x/q
   int64_t tot_lines = 0, tot_ch = 0, packed_elems = 0;
   int max_res = 0, max_pairs = 0;
+  bool all_resident = true;  // every frame entirely in shared memory (tuner class 1)
 };
 
 // Frame table of a streamline launch: padded sizes, packed offsets (FP32C
@@ -441,6 +442,7 @@ int build_topo_tables(int prec, int F, const int64_t* desc, const double* params
     fr.step = pr[0];
     for (int k = 0; k < 3; ++k) fr.half[k] = pr[1 + k];
     t.max_res = std::max(t.max_res, int(fr.resident));
+    if (fr.resident < fr.n_pad) t.all_resident = false;
     t.max_pairs = std::max(t.max_pairs, int(fr.n_pad));
     t.src[2 * f] = co;
     t.src[2 * f + 1] = n;
@@ -462,6 +464,7 @@ int topo_batch_impl(int prec, int mem, int F, const int64_t* desc, const double*
   std::vector<int64_t>& src = t.src;
   const int64_t tot_lines = t.tot_lines, tot_ch = t.tot_ch, packed_elems = t.packed_elems;
   const int max_res = t.max_res, max_pairs = t.max_pairs;
+  const bool all_resident = t.all_resident;
   if (tot_lines == 0) return CPETGB_OK;
   if (!starts || !n_iter || !result) return fail(CPETGB_EINVAL, "line pointer is NULL");
   if (tot_ch > 0 && (!x || !q)) return fail(CPETGB_EINVAL, "charge pointer is NULL");
@@ -514,6 +517,7 @@ int topo_batch_impl(int prec, int mem, int F, const int64_t* desc, const double*
   p.frames = d_frames;
   p.n_frames = F;
   p.max_resident_pad = max_res;
+  p.all_resident = all_resident ? 1 : 0;
   CK(launch_topo_frames(prec, p, c->sms, s), "topo kernel launch");
   if (mem == CPETGB_HOST) {
     CK(cudaMemcpyAsync(result, dres, L * 2 * sizeof(double), cudaMemcpyDeviceToHost, s),
@@ -929,6 +933,7 @@ int topo_plan_impl(cpetgb_plan** out_plan, int prec, int F, const int64_t* desc,
   p.frames = d_frames;
   p.n_frames = F;
   p.max_resident_pad = t.max_res;
+  p.all_resident = t.all_resident ? 1 : 0;
   const int max_pairs = t.max_pairs;
   rc = capture_plan(pl, [&](cudaStream_t cs) -> int {
     CK(cudaMemsetAsync(queues, 0, sizeof(int) * size_t(std::max(F, 1)), cs), "zero queues");

@@ -105,6 +105,7 @@ struct TopoParams {
   const TopoFrame* frames;   // device frame table (multi-frame launches) or null
   int n_frames;              // frames in the table
   int max_resident_pad;      // largest TopoFrame::resident of the launch (shared-memory size)
+  int all_resident = 0;      // 1: every frame entirely in shared memory (tuner class)
   int source = kCharges;     // kDipoles: packed holds dipoles (single-frame launches only)
 };
 // Single frame: p.frames == null, the frame is described by n_charges/step/half.

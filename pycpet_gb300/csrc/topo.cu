@@ -27,8 +27,10 @@
 //     without any block-wide synchronisation, so short and long lines mix.
 //
 // Precision forms:
-//   FP32C  charges are float4 (x,y,z,q) held resident in shared memory (one
-//          bulk async copy per CTA); pair terms in FP32 with the MUFU rsqrt,
+//   FP32C  charges in pairs of float4 records held in shared memory (bulk
+//          async copies per CTA; a frame larger than shared memory keeps a
+//          prefix there and streams the rest from L2); pair terms in FP32 with
+//          the MUFU rsqrt,
 //          per-lane Kahan accumulation across charge tiles and an error-free
 //          (TwoSum) warp reduction; the step vector is formed in FP32 and added
 //          to an FP64 position; box test, curvature and distance in FP64.
@@ -1165,7 +1167,7 @@ cudaError_t launch_topo(int prec, const TopoParams& p_in, int num_sms, cudaStrea
 cudaError_t launch_topo_frames(int prec, const TopoParams& p, int num_sms, cudaStream_t s) {
   if (p.n_frames <= 0 || p.n_lines <= 0) return cudaSuccess;
   TopoFrame dummy{};
-  const int slots = tuned_topo_slots(prec, p.max_resident_pad > 0, p.n_lines);
+  const int slots = tuned_topo_slots(prec, p.all_resident != 0, p.n_lines);
   if (prec == kFP64) return launch_topo_s<kFP64, false>(p, dummy, p.n_lines, num_sms, s, slots);
   if (p.max_resident_pad > 0)
     return launch_topo_s<kFP32C, true>(p, dummy, p.n_lines, num_sms, s, slots);
