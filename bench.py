@@ -416,6 +416,60 @@ def grid_main(args, rank, world, dev, torch, dist):
         dist.destroy_process_group()
 
 
+def engine_throughput(frames, rank, torch, n_req=100):
+    """Streamline-only burst through the serving engine: n_req requests of
+    500-1,500 lines (step 0.001 A, cap 6,000), all queued at once, on the
+    10,000-charge frame and on the mix of 2,000-100,000-charge frames; the
+    engine at one CTA per SM (half of every SM, the mixed-serving setting) and
+    at two (whole SMs), beside one batched launch of the same lines
+    (cpetgb_topo_batch).  Lines/s and pair evaluations/s from the step counts."""
+    from dataclasses import replace
+
+    from pycpet_gb300.core import TopoBatch
+    from pycpet_gb300.serving import Request, Server
+
+    out = {}
+    for name, fids in (("10000_charges", [2]), ("2000-100000_charges", list(frames))):
+        rng = np.random.default_rng(4242 + rank)
+        reqs = []
+        for i in range(n_req):
+            f = int(fids[int(rng.integers(0, len(fids)))])
+            L = int(rng.integers(500, 1501))
+            reqs.append(Request("topo", f, 0.0, starts=rng.uniform(-1.5, 1.5, (L, 3)), n_iter=6000, step=0.001))
+        tb = TopoBatch([{"x": frames[r.frame]["x"], "q": frames[r.frame]["q"], "starts": r.starts,
+                         "n_iter": 6000, "step": 0.001, "half_dims": [1.5] * 3} for r in reqs],
+                       precision="fp32c", device=True)
+        res, steps = tb.run(return_steps=True)
+        torch.cuda.synchronize()
+        steps = steps.cpu().numpy()
+        n_of = np.concatenate([np.full(len(r.starts), len(frames[r.frame]["q"]), np.int64) for r in reqs])
+        pe = int(np.sum((np.maximum(steps, 2) + 2).astype(np.int64) * n_of))
+        n_lines = len(steps)
+        t0 = time.perf_counter()
+        tb.run()
+        torch.cuda.synchronize()
+        t_batch = time.perf_counter() - t0
+        row = {"requests": n_req, "lines": n_lines, "pair_evals": pe,
+               "batch_launch": {"s": t_batch, "lines_per_s": n_lines / t_batch, "pair_evals_per_s": pe / t_batch}}
+        ref = res.cpu().numpy()
+        for cps in (1, 2):
+            srv = Server(precision="fp32c", line_capacity=2_000_000, charge_capacity=400_000, max_requests=4096,
+                         engine_ctas_per_sm=cps)
+            for fid, fr in frames.items():
+                srv.add_frame(fid, fr["x"], fr["q"])
+            srv.run([Request("topo", r.frame, 0.0, starts=r.starts[:64], n_iter=6000, step=0.001) for r in reqs[:8]])
+            burst = [replace(r, result=None, t_start=None, t_done=None, _rid=-1) for r in reqs]
+            t0 = time.perf_counter()
+            srv.run(burst)
+            t = time.perf_counter() - t0
+            srv.close()
+            same = bool(np.array_equal(np.concatenate([r.result for r in burst]), ref))
+            row[f"engine_{cps}_cta_per_sm"] = {"s": t, "lines_per_s": n_lines / t, "pair_evals_per_s": pe / t,
+                                               "identical_to_batch": same}
+        out[name] = row
+    return out
+
+
 def serve_main(args, rank, world, dev, torch, dist):
     """--workload serve: Poisson arrivals mixing point_field (1-64 points),
     volume / volume_ESP (11^3-51^3) and topo requests on resident frames of
@@ -457,6 +511,7 @@ def serve_main(args, rank, world, dev, torch, dist):
                          "grid_pair_evals": pe, "latency": stats,
                          "max_topo_requests_in_flight": srv.max_topo_inflight}
         srv.close()
+    out["streamline_throughput"] = engine_throughput(frames, rank, torch)
     out["value"] = results["fp32c"]["requests_per_s"]
     out["ms_per_step"] = 1e3 * results["fp32c"]["wall_s"]
     out["config"] = {"workload": f"serving: Poisson arrivals at {args.rate:g}/s, point_field 1-64 points, "

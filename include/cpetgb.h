@@ -200,6 +200,11 @@ int cpetgb_engine_submit(cpetgb_engine* engine, int frame_id, int n_lines, const
 int cpetgb_engine_poll(cpetgb_engine* engine, int request_id);  /* 1 done, 0 pending */
 int cpetgb_engine_collect(cpetgb_engine* engine, int request_id, double* result, int32_t* steps);
 int cpetgb_engine_drain(cpetgb_engine* engine);
+/* Engine CTAs per SM from its next launch on: 1 (default) takes half of every
+ * SM's registers, so grid and point launches on other streams run beside the
+ * engine; 2 gives the engine whole SMs (higher streamline throughput, but grid
+ * launches wait until the engine's launch ends). */
+int cpetgb_engine_set_ctas_per_sm(cpetgb_engine* engine, int ctas_per_sm);
 
 /* Streamlines for callers that must not have device memory allocated on their
  * behalf (device memory reserved up front by their own allocator, or a fixed

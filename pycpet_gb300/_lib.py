@@ -68,6 +68,7 @@ SIGNATURES = {
     "cpetgb_engine_poll": [_vp, _i],
     "cpetgb_engine_collect": [_vp, _i, _vp, _vp],
     "cpetgb_engine_drain": [_vp],
+    "cpetgb_engine_set_ctas_per_sm": [_vp, _i],
     "cpetgb_topo_lines_noalloc": [_i, _i, _i, _vp, _vp, _d, _vp, _vp, _vp, _vp, _vp, _vp, _vp],
     "cpetgb_topo_hist2d": [_i, _i, _vp, _i, _i, _vp, _vp, _vp, _vp],
     "cpetgb_prepare_frame": [_i, _i, _vp, _vp, _vp, _vp, _vp, _vp, _d, _vp, _vp, _vp, _vp, _vp, _vp],

@@ -11,8 +11,9 @@
 //    returns CPETGB_EAGAIN and the caller retries after collecting others.
 // Launch rule: after publishing, if fewer than two engine launches are in
 // flight one more is queued on the engine stream.  A running kernel takes the
-// new chunks as its slots free up; a queued one starts when it ends, so work
-// is never left unclaimed.  Storage released by collect/remove is reused only
+// new chunks as its slots free up (its idle warps stay while any of its warps
+// has lines); once it has been idle for 50 ms it closes and ends, and a queued
+// one starts, so work is never left unclaimed.  Storage released by collect/remove is reused only
 // when no engine launch is in flight (the kernel may hold it in L1).
 #include <algorithm>
 #include <cmath>
@@ -89,6 +90,7 @@ struct FrameSlot {
 
 struct cpetgb_engine {
   int device = -1, prec = CPETGB_FP32C, sms = 0;
+  int ctas_per_sm = 1;  // 1: half of every SM's registers; 2: whole SMs
   int chunk_lines = 32;
   cudaStream_t run_stream = nullptr, copy_stream = nullptr;
   std::mutex mu;
@@ -100,7 +102,7 @@ struct cpetgb_engine {
   double* result = nullptr;
   int32_t* steps = nullptr;
   int* status = nullptr;
-  int* d_head = nullptr;      // claim counter (device)
+  int* d_head = nullptr;      // [0] claim counter, [1] busy warps, [2] closing flag (device)
   double* stage_x = nullptr;  // frame upload staging
   double* stage_q = nullptr;
   int64_t stage_cap = 0;
@@ -170,7 +172,12 @@ struct cpetgb_engine {
     E.head = d_head;
     E.head_mirror = d_counters + 1;
     E.done = d_done;
-    cudaError_t e = launch_engine(prec, E, sms, run_stream);
+    E.busy = d_head + 1;
+    E.closing = d_head + 2;
+    // the launch's busy count and closing flag start at 0 (stream-ordered after
+    // the previous launch)
+    cudaError_t e = cudaMemsetAsync(d_head + 1, 0, 2 * sizeof(int), run_stream);
+    if (e == cudaSuccess) e = launch_engine(prec, E, sms * ctas_per_sm, run_stream);
     if (e != cudaSuccess) return e;
     cudaEvent_t ev;
     e = cudaEventCreateWithFlags(&ev, cudaEventDisableTiming);
@@ -248,8 +255,8 @@ int cpetgb_engine_create(cpetgb_engine** out, int precision, int64_t charge_capa
   if (err == cudaSuccess) err = cudaMalloc(&e->steps, sizeof(int32_t) * line_capacity);
   if (err == cudaSuccess) err = cudaMalloc(&e->status, sizeof(int));
   if (err == cudaSuccess) err = cudaMemset(e->status, 0, sizeof(int));
-  if (err == cudaSuccess) err = cudaMalloc(&e->d_head, sizeof(int));
-  if (err == cudaSuccess) err = cudaMemset(e->d_head, 0, sizeof(int));
+  if (err == cudaSuccess) err = cudaMalloc(&e->d_head, 3 * sizeof(int));
+  if (err == cudaSuccess) err = cudaMemset(e->d_head, 0, 3 * sizeof(int));
   if (err == cudaSuccess)
     err = cudaHostAlloc(&e->chunks, sizeof(EngineChunk) * e->chunk_cap, cudaHostAllocMapped);
   if (err == cudaSuccess) err = cudaHostAlloc(&e->counters, sizeof(int) * 2, cudaHostAllocMapped);
@@ -355,7 +362,7 @@ int cpetgb_engine_submit(cpetgb_engine* e, int frame_id, int n_lines, const doub
   if (rid < 0) return efail(CPETGB_EAGAIN, "all request slots are in use");
   // chunk size: spread the request over every warp of the engine (at least one
   // warp's line slots per chunk, at most chunk_lines)
-  const int warps = e->sms * (engine_threads() / 32);
+  const int warps = e->sms * e->ctas_per_sm * (engine_threads() / 32);
   const int cl = std::max(4, std::min(e->chunk_lines, n_lines / std::max(warps, 1)));
   const int n_chunks = (n_lines + cl - 1) / cl;
   const int claimed = __atomic_load_n(e->counters + 1, __ATOMIC_ACQUIRE);
@@ -426,6 +433,16 @@ int cpetgb_engine_collect(cpetgb_engine* e, int request_id, double* result, int3
   ECK(cudaStreamSynchronize(e->copy_stream), "result download");
   e->line_pool.release(r.line_begin, r.n_lines);
   r.used = false;
+  return CPETGB_OK;
+}
+
+// Engine CTAs per SM from the next launch on: 1 leaves half of every SM's
+// registers to grid launches on other streams; 2 gives the engine whole SMs.
+int cpetgb_engine_set_ctas_per_sm(cpetgb_engine* e, int ctas_per_sm) {
+  if (!e) return efail(CPETGB_EINVAL, "engine is NULL");
+  if (ctas_per_sm != 1 && ctas_per_sm != 2) return efail(CPETGB_EINVAL, "ctas_per_sm must be 1 or 2");
+  std::lock_guard<std::mutex> lock(e->mu);
+  e->ctas_per_sm = ctas_per_sm;
   return CPETGB_OK;
 }
 

@@ -156,6 +156,8 @@ struct EngineParams {
   int* head;                    // chunks claimed (device memory)
   int* head_mirror;             // claims seen by the host (host-mapped, monotonic)
   int* done;                    // finished lines per request slot (host-mapped)
+  int* busy;                    // warps of this launch holding lines (device memory, 0 at launch)
+  int* closing;                 // 1 once this launch takes no more chunks (device memory, 0 at launch)
 };
 cudaError_t launch_engine(int prec, const EngineParams& e, int ctas, cudaStream_t s);
 int engine_threads();

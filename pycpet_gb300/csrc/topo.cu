@@ -648,12 +648,20 @@ __global__ void __launch_bounds__(kTopoThreads, 1) topo_kernel(TopoParams p, Top
 // chunk (or of a newly claimed chunk, possibly of another frame), so requests
 // arriving while others are in flight are admitted as slots free up.  Each
 // step the warp sweeps the charges once per distinct frame among its active
-// slots.  Charges are read from global memory (L2).  Nothing waits: a warp
-// that finds no line and no chunk exits; the host launches a new kernel when
-// it publishes work after the previous one may have ended.
+// slots.  Charges are read from global memory (L2).
+//
+// Lifetime of a launch: a warp without lines polls for chunks, and stays while
+// any warp of the launch has lines or claims happen, so work published later
+// finds every warp of the launch (a launch whose idle warps had left would
+// serve it with the few warps still busy, while the next launch waits behind
+// it).  Once no warp has had lines and nothing was claimed for kEngineIdleNs,
+// the first warp to see it closes the launch: no warp claims again, and each
+// ends when its lines are done.  Work published after that goes to the next
+// launch, which the host keeps queued.
 constexpr int kEngineThreads = 256;
 constexpr int kEngineWarps = kEngineThreads / 32;
-constexpr unsigned long long kEngineIdleNs = 50000000ull;  // 50 ms of polling before a warp exits
+constexpr unsigned long long kEngineIdleNs = 50000000ull;      // launch idle 50 ms: it closes
+constexpr unsigned long long kEngineMaxWaitNs = 60000000000ull;  // bound on one idle wait (60 s)
 
 __device__ __forceinline__ int ld_acquire_sys(const int* p) {
   int v;
@@ -676,6 +684,39 @@ __device__ int engine_claim(const EngineParams& E) {
     }
   }
   return -1;
+}
+
+__device__ __forceinline__ int ld_volatile(const int* p) { return *reinterpret_cast<const volatile int*>(p); }
+
+// Idle wait of a warp with no line (lane 0 only): polls for a chunk with a
+// sleep growing from 20 to 320 us.  Returns the claimed chunk, or -1 once the
+// launch is closed -- by this warp when neither a busy warp nor a claim was
+// seen for kEngineIdleNs, or after kEngineMaxWaitNs in any case.
+__device__ int engine_idle_wait(const EngineParams& E) {
+  const unsigned long long t0 = globaltimer_ns();
+  unsigned long long quiet_since = t0;
+  int last_head = ld_volatile(E.head);
+  unsigned sleep_ns = 20000;
+  for (;;) {
+    if (ld_volatile(E.closing)) return -1;
+    const int got = engine_claim(E);
+    if (got >= 0) return got;
+    const unsigned long long now = globaltimer_ns();
+    const int h = ld_volatile(E.head);
+    if (ld_volatile(E.busy) > 0 || h != last_head) {
+      quiet_since = now;
+      last_head = h;
+    } else if (now - quiet_since > kEngineIdleNs) {
+      atomicExch(E.closing, 1);
+      return -1;
+    }
+    if (now - t0 > kEngineMaxWaitNs) {
+      atomicExch(E.closing, 1);
+      return -1;
+    }
+    __nanosleep(sleep_ns);
+    if (sleep_ns < 320000) sleep_ns *= 2;
+  }
 }
 
 __device__ __forceinline__ EngineChunk engine_read_chunk(const EngineParams& E, int idx) {
@@ -744,31 +785,29 @@ __global__ void __launch_bounds__(kEngineThreads, 2) engine_kernel(EngineParams 
   sl.posf[0] = sl.posf[1] = sl.posf[2] = 0.f;
   int c_next = 0, c_end = 0;  // the warp's chunk cursor (uniform across the warp)
   int backoff = 0;            // steps to wait before claiming again after an empty queue
+  bool counted = false;       // this warp is counted in E.busy (uniform)
   __syncwarp();
 
   for (;;) {
     // refill idle slots, claiming chunks as needed
     unsigned need = __ballot_sync(0xffffffffu, lane < S && sl.line < 0);
     const bool all_idle = __popc(need) == S;
+    if (all_idle && counted && c_next >= c_end) {  // no line held or left in the chunk
+      if (lane == 0) atomicSub(E.busy, 1);
+      counted = false;
+    }
     if (backoff > 0 && !all_idle) {
       --backoff;
       need = (c_next < c_end) ? need : 0u;  // only lines of the current chunk
     }
+    bool took = false;  // a line was given to a slot in this pass
     while (need) {
       if (c_next >= c_end) {
         int got = -1;
         if (lane == 0) {
-          got = engine_claim(E);
-          // A warp with nothing to do polls for new chunks for a bounded time
-          // (kEngineIdleNs) before it exits, so the kernel keeps its warps
-          // between arrivals instead of thinning out.
-          if (got < 0 && all_idle) {
-            const unsigned long long t0 = globaltimer_ns();
-            while (got < 0 && globaltimer_ns() - t0 < kEngineIdleNs) {
-              __nanosleep(20000);
-              got = engine_claim(E);
-            }
-          }
+          if (!ld_volatile(E.closing)) got = engine_claim(E);
+          if (got < 0 && all_idle && !took) got = engine_idle_wait(E);
+          if (got >= 0 && !counted) atomicAdd(E.busy, 1);
           if (got >= 0) wchunk[warp] = engine_read_chunk(E, got);
         }
         got = __shfl_sync(0xffffffffu, got, 0);
@@ -777,6 +816,7 @@ __global__ void __launch_bounds__(kEngineThreads, 2) engine_kernel(EngineParams 
           backoff = 8;
           break;
         }
+        counted = true;
         c_next = wchunk[warp].line_begin;
         c_end = wchunk[warp].line_end;
         continue;
@@ -794,6 +834,7 @@ __global__ void __launch_bounds__(kEngineThreads, 2) engine_kernel(EngineParams 
         for (int k = 0; k < 3; ++k) my.half[k] = ch.half[k];
         engine_slot_load(sl, rec, line, E.p);
       }
+      took = true;
       need &= ~(1u << target);
       __syncwarp();
     }
@@ -1049,8 +1090,10 @@ int topo_charge_pad(int prec) { return prec == kFP32C ? kChargePad32 : kChargePa
 
 int engine_threads() { return kEngineThreads; }
 
-// The engine runs beside grid launches: its SMs keep the largest shared-memory
-// carveout so grid blocks (33 KB of staged charge tiles) fit next to it.
+// ctas = SMs x CTAs per SM (1 or 2; a CTA takes half of an SM's registers).
+// At one CTA per SM the engine runs beside grid launches: its SMs keep the
+// largest shared-memory carveout so grid blocks (33 KB of staged charge
+// tiles) fit next to it.
 cudaError_t launch_engine(int prec, const EngineParams& e, int ctas, cudaStream_t s) {
   cudaError_t err;
   if (prec == kFP32C) {

@@ -10,7 +10,8 @@ time against frames whose charges stay resident on the device.
 * Grid and point requests that are waiting are batched into one
   descriptor-table launch per kind (field with the r^2 clamp, unclamped point
   fields, potential) on one of two side streams, beside the engine kernel
-  (which leaves half of every SM's registers free for them).
+  (which, at one CTA per SM, leaves half of every SM's registers free for
+  them; a streamline-only server gives the engine two).
 * Admission: a request is started only while the memory it needs fits an HBM
   budget (80% of the device by default) next to the resident frames; the
   engine also refuses (and the loop retries) when its line store is full.
@@ -70,7 +71,12 @@ class _GridLaunch:
 
 class Server:
     def __init__(self, precision="fp32c", hbm_budget_frac=0.8, line_capacity=2_000_000,
-                 charge_capacity=4_000_000, max_frames=64, max_requests=4096, chunk_lines=32):
+                 charge_capacity=4_000_000, max_frames=64, max_requests=4096, chunk_lines=32,
+                 engine_ctas_per_sm=1):
+        """``engine_ctas_per_sm``: 1 keeps half of every SM free for grid and
+        point requests (mixed serving); 2 gives the streamline engine whole SMs
+        (streamline-only serving: about 1.5x the line throughput, but a grid
+        request then waits until the engine's launch ends)."""
         import torch
 
         self.torch = torch
@@ -85,6 +91,7 @@ class Server:
         check(lib().cpetgb_engine_create(ctypes.byref(h), self.prec, int(charge_capacity), int(line_capacity),
                                          int(max_frames), int(max_requests), int(chunk_lines)))
         self.engine = h
+        check(lib().cpetgb_engine_set_ctas_per_sm(h, int(engine_ctas_per_sm)))
         self.resident_bytes += int(charge_capacity * 32 + line_capacity * 56)
         self.frames = {}          # frame id -> dict(engine id, offset in the grid pool, n)
         self._gx, self._gq = [], []

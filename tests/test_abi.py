@@ -97,6 +97,7 @@ def test_argument_validation_new_entry_points(built):
     assert "resid" in _lib.last_error()
     assert L.cpetgb_topo_dipole_lines(5, 0, 1, 1, x.ctypes.data, None, 0.1, c.ctypes.data, x.ctypes.data,
                                       x.ctypes.data, out.ctypes.data, None, None, None) == _lib.EINVAL
+    assert L.cpetgb_engine_set_ctas_per_sm(None, 2) == _lib.EINVAL
 
 
 def test_tuning_table_round_trip(built):

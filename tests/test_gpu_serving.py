@@ -74,6 +74,74 @@ def test_same_alone_and_in_mix(gpu_lib, precision):
     srv.close()
 
 
+def test_engine_on_whole_sms(gpu_lib):
+    """Two engine CTAs per SM (whole SMs for streamlines): results identical
+    to cpetgb_topo_lines; a third value is refused."""
+    from pycpet_gb300 import _lib, topo_lines
+    from pycpet_gb300.serving import Request, Server
+
+    frames = _frames()
+    srv = Server(line_capacity=100_000, charge_capacity=100_000, max_requests=64, engine_ctas_per_sm=2)
+    for fid, fr in frames.items():
+        srv.add_frame(fid, fr["x"], fr["q"])
+    rng = np.random.default_rng(11)
+    reqs = []
+    for i in range(6):
+        L = int(rng.integers(50, 3000))
+        reqs.append(Request("topo", i % 3, 0.0, starts=rng.uniform(-1.5, 1.5, (L, 3)),
+                            n_iter=rng.integers(0, 300, L).astype(np.int32), step=0.01))
+    srv.run(reqs)
+    for r in reqs:
+        fr = frames[r.frame]
+        np.testing.assert_array_equal(r.result, topo_lines(r.starts, r.n_iter, fr["x"], fr["q"], r.step, r.half_dims))
+    assert _lib.lib().cpetgb_engine_set_ctas_per_sm(srv.engine, 3) == _lib.EINVAL
+    srv.close()
+
+
+@pytest.mark.parametrize("ctas_per_sm", [1, 2])
+def test_burst_right_after_a_run_uses_every_warp(gpu_lib, ctas_per_sm):
+    """A burst submitted while the previous engine launch is still alive (its
+    warps idle after a small request) is served by all of that launch's warps:
+    it takes about as long as the same burst on an engine that had ended
+    (a launch whose idle warps had left served such a burst with its few busy
+    warps, several times slower), with identical results."""
+    import time
+
+    from pycpet_gb300 import _lib, topo_lines
+    from pycpet_gb300.serving import Request, Server
+
+    fr = _frames()[1]
+    srv = Server(line_capacity=200_000, charge_capacity=100_000, max_requests=256, engine_ctas_per_sm=ctas_per_sm)
+    srv.add_frame(0, fr["x"], fr["q"])
+    rng = np.random.default_rng(3)
+    base = [Request("topo", 0, 0.0, starts=rng.uniform(-1.5, 1.5, (600, 3)), n_iter=2000, step=0.001)
+            for _ in range(40)]
+    # a few long lines (about 20,000 steps of 1e-4 A): the launch outlives the
+    # 50 ms idle period of its other warps
+    small = Request("topo", 0, 0.0, starts=rng.uniform(-0.2, 0.2, (8, 3)), n_iter=20000, step=0.0001)
+
+    def timed(reqs):
+        t0 = time.perf_counter()
+        srv.run(reqs)
+        return time.perf_counter() - t0
+
+    timed([_clone(r) for r in base])                      # warm-up
+    _lib.check(_lib.lib().cpetgb_engine_drain(srv.engine))
+    cold = [_clone(r) for r in base]
+    t_cold = timed(cold)                                  # on an engine that had ended
+    _lib.check(_lib.lib().cpetgb_engine_drain(srv.engine))
+    srv.run([_clone(small)])
+    hot = [_clone(r) for r in base]
+    t_hot = timed(hot)                                    # right after a small run
+    srv.close()
+    for a, b in zip(cold, hot):
+        np.testing.assert_array_equal(a.result, b.result)
+    r0 = base[0]
+    np.testing.assert_array_equal(hot[0].result, topo_lines(r0.starts, r0.n_iter, fr["x"], fr["q"], r0.step,
+                                                            r0.half_dims))
+    assert t_hot < 2.0 * t_cold + 0.1, (t_hot, t_cold)
+
+
 def test_admission_retries_when_full(gpu_lib):
     """A line store smaller than the queued work: requests wait for capacity
     and all finish with the right results."""
