@@ -264,13 +264,19 @@ __device__ __forceinline__ void dipole_run(const ulonglong2* __restrict__ A,
   }
 }
 
-// Pairs [0, res_pairs) are read from (sA, sB, sC) -- the shared-memory copy of
-// a frame's first pairs -- and pairs [res_pairs, n_pairs) from (A, B, C) in
-// global memory (L2).  res_pairs is n_pairs (all resident), 0 (none) or a
-// multiple of the 32 x kLanePairs pairs of one Kahan run, so every run reads
-// one source and the sums are the same whichever part is resident.
+// Sources of a sweep.  kSrcOne: every pair from (A, B, C) -- a frame held
+// entirely in shared memory, or one read entirely from global memory.
+// kSrcSplit: pairs [0, res_pairs) from (sA, sB, sC), the shared-memory copy of
+// a frame's first pairs, the rest from (A, B, C) in global memory (L2);
+// res_pairs is a multiple of the 32 x kLanePairs pairs of one Kahan run, so
+// every run reads one source and the sums are the same whichever part is
+// resident.  The single-source loop is compiled on its own: with both sources
+// in one loop the all-resident sweep ran 12% slower.
+constexpr int kSrcOne = 0;
+constexpr int kSrcSplit = 1;
+
 // DIP: point dipoles (dipole_run, C used); otherwise point charges (pair_run).
-template <int NA, int S, bool DIP = false>
+template <int NA, int S, bool DIP = false, int SRC = kSrcOne>
 __device__ __forceinline__ void sweep_f32x2(const ulonglong2* __restrict__ sA,
                                             const ulonglong2* __restrict__ sB,
                                             const ulonglong2* __restrict__ sC, int res_pairs,
@@ -295,7 +301,7 @@ __device__ __forceinline__ void sweep_f32x2(const ulonglong2* __restrict__ sA,
     // about eight independent pair chains in flight per lane: unroll 8 / NA
     constexpr int kUnroll = NA >= 3 ? 2 : (NA == 2 ? 4 : 8);
     const int cnt = left >= kLanePairs ? kLanePairs : left;
-    if (base < res_pairs) {  // shared-memory copy
+    if (SRC == kSrcSplit && base < res_pairs) {  // shared-memory copy
       if constexpr (DIP) {
         if (cnt == kLanePairs)
           dipole_run<NA, S, kUnroll>(sA, sB, sC, base + lane, kLanePairs, ex2, part);
@@ -307,7 +313,7 @@ __device__ __forceinline__ void sweep_f32x2(const ulonglong2* __restrict__ sA,
         else
           pair_run<NA, S, 1>(sA, sB, base + lane, cnt, ex2, part);
       }
-    } else {  // global memory
+    } else {  // global memory (kSrcSplit), or the one source
       if constexpr (DIP) {
         if (cnt == kLanePairs)
           dipole_run<NA, S, kUnroll>(A, B, C, base + lane, kLanePairs, ex2, part);
@@ -445,15 +451,48 @@ __device__ __forceinline__ void sweep_dipole_f64(const Dipole64* __restrict__ g,
 // Persistent kernel.
 // ---------------------------------------------------------------------------
 
+// Residency of a launch's frames (kernel template RES): kResNone -- every
+// frame read from global memory (L2); kResWhole -- each frame entirely in
+// shared memory or read from L2; kResAny -- also frames of which only a prefix
+// is resident (frames above the shared-memory limit).  The prefix sweeps are
+// compiled only into kResAny kernels: with them in the kernel of whole-frame
+// launches its instruction cache missed (no-instruction stalls 0.31 per issue
+// instead of 0.05) and the 8,000-charge workload ran 6% slower.
+constexpr int kResNone = 0;
+constexpr int kResWhole = 1;
+constexpr int kResAny = 2;
+
+// The sweep of one frame of a kResAny launch: res_pairs of its n_pairs pairs
+// are in shared memory.
+template <int NA, int S, bool DIP>
+__device__ __forceinline__ void sweep_frame_any(const ulonglong2* smA, const ulonglong2* smB,
+                                                const ulonglong2* smC, int res_pairs,
+                                                const ulonglong2* chA, const ulonglong2* chB,
+                                                const ulonglong2* chC, int n_pairs, int lane,
+                                                const uint64_t (&ex2)[S][3], float& total) {
+  if (res_pairs >= n_pairs)
+    sweep_f32x2<NA, S, DIP, kSrcOne>(nullptr, nullptr, nullptr, 0, smA, smB, smC, n_pairs, lane, ex2,
+                                     total);
+  else if (res_pairs > 0)
+    sweep_f32x2<NA, S, DIP, kSrcSplit>(smA, smB, smC, res_pairs, chA, chB, chC, n_pairs, lane, ex2,
+                                       total);
+  else
+    sweep_f32x2<NA, S, DIP, kSrcOne>(nullptr, nullptr, nullptr, 0, chA, chB, chC, n_pairs, lane, ex2,
+                                     total);
+}
+
 // One line slot set per warp; processes the lines of frame `fc` (charge
 // arrays chA/chB in the FP32C pair layout, or g in Charge64) until the frame's
 // queue is exhausted and the warp's slots are drained.
-template <int PREC, int S, bool DIP>
+// resident: the whole frame is in shared memory (kResWhole launches);
+// res_pairs: pairs in shared memory (kResAny launches).
+template <int PREC, int S, bool DIP, int RES>
 __device__ __forceinline__ void run_frame(const TopoParams& p, const FrameCtx& fc, int* queue,
                                           const ulonglong2* chA, const ulonglong2* chB,
                                           const ulonglong2* chC, const ulonglong2* smA,
                                           const ulonglong2* smB, const ulonglong2* smC,
-                                          int res_pairs, int n_pad, SlotRec* my_rec, int lane) {
+                                          bool resident, int res_pairs, int n_pad, SlotRec* my_rec,
+                                          int lane) {
   Slot sl;
   sl.line = -1;
   sl.phase = kMain;
@@ -493,20 +532,36 @@ __device__ __forceinline__ void run_frame(const TopoParams& p, const FrameCtx& f
         }
       float total;
       const int n_pairs = n_pad / 2;
-      switch (na) {
-        case 1:
-          sweep_f32x2<1, S, DIP>(smA, smB, smC, res_pairs, chA, chB, chC, n_pairs, lane, ex2, total);
-          break;
-        case 2:
-          sweep_f32x2<2, S, DIP>(smA, smB, smC, res_pairs, chA, chB, chC, n_pairs, lane, ex2, total);
-          break;
-        case 3:
-          sweep_f32x2<(S > 2 ? 3 : 2), S, DIP>(smA, smB, smC, res_pairs, chA, chB, chC, n_pairs, lane,
-                                               ex2, total);
-          break;
-        default:
-          sweep_f32x2<S, S, DIP>(smA, smB, smC, res_pairs, chA, chB, chC, n_pairs, lane, ex2, total);
-          break;
+      if constexpr (RES == kResAny) {
+        switch (na) {
+          case 1:
+            sweep_frame_any<1, S, DIP>(smA, smB, smC, res_pairs, chA, chB, chC, n_pairs, lane, ex2, total);
+            break;
+          case 2:
+            sweep_frame_any<2, S, DIP>(smA, smB, smC, res_pairs, chA, chB, chC, n_pairs, lane, ex2, total);
+            break;
+          case 3:
+            sweep_frame_any<(S > 2 ? 3 : 2), S, DIP>(smA, smB, smC, res_pairs, chA, chB, chC, n_pairs,
+                                                     lane, ex2, total);
+            break;
+          default:
+            sweep_frame_any<S, S, DIP>(smA, smB, smC, res_pairs, chA, chB, chC, n_pairs, lane, ex2, total);
+            break;
+        }
+      } else if (resident) {  // whole frame in shared memory
+        switch (na) {
+          case 1: sweep_f32x2<1, S, DIP>(nullptr, nullptr, nullptr, 0, smA, smB, smC, n_pairs, lane, ex2, total); break;
+          case 2: sweep_f32x2<2, S, DIP>(nullptr, nullptr, nullptr, 0, smA, smB, smC, n_pairs, lane, ex2, total); break;
+          case 3: sweep_f32x2<(S > 2 ? 3 : 2), S, DIP>(nullptr, nullptr, nullptr, 0, smA, smB, smC, n_pairs, lane, ex2, total); break;
+          default: sweep_f32x2<S, S, DIP>(nullptr, nullptr, nullptr, 0, smA, smB, smC, n_pairs, lane, ex2, total); break;
+        }
+      } else {  // every pair from global memory
+        switch (na) {
+          case 1: sweep_f32x2<1, S, DIP>(nullptr, nullptr, nullptr, 0, chA, chB, chC, n_pairs, lane, ex2, total); break;
+          case 2: sweep_f32x2<2, S, DIP>(nullptr, nullptr, nullptr, 0, chA, chB, chC, n_pairs, lane, ex2, total); break;
+          case 3: sweep_f32x2<(S > 2 ? 3 : 2), S, DIP>(nullptr, nullptr, nullptr, 0, chA, chB, chC, n_pairs, lane, ex2, total); break;
+          default: sweep_f32x2<S, S, DIP>(nullptr, nullptr, nullptr, 0, chA, chB, chC, n_pairs, lane, ex2, total); break;
+        }
       }
       // component c of slot rank e sits in lanes (3e + c) << (5 - LV) and up
       float Ef[3];
@@ -573,8 +628,9 @@ __device__ __forceinline__ void run_frame(const TopoParams& p, const FrameCtx& f
 // copy of the charges can be replaced).  Frames thus overlap only at their
 // tails and every frame switch costs a CTA one line's latency at most.
 // DIP: the sources are point dipoles (FP32C: three 16-byte pair blocks per
-// frame; FP64: Dipole64 records) instead of point charges.
-template <int PREC, bool CAN_RESIDE, int S, bool DIP>
+// frame; FP64: Dipole64 records) instead of point charges.  RES: residency
+// mode of the launch's frames (kResNone, kResWhole, kResAny).
+template <int PREC, int RES, int S, bool DIP>
 __global__ void __launch_bounds__(kTopoThreads, 1) topo_kernel(TopoParams p, TopoFrame frame0) {
   extern __shared__ __align__(128) unsigned char smem_raw[];
   __shared__ int s_skip;
@@ -587,7 +643,7 @@ __global__ void __launch_bounds__(kTopoThreads, 1) topo_kernel(TopoParams p, Top
   SlotRec* my_rec = recs + warp * S + (lane < S ? lane : 0);
   const int n_frames = p.frames ? p.n_frames : 1;
   uint32_t load_parity = 0;
-  if (CAN_RESIDE && threadIdx.x == 0) {
+  if (RES != kResNone && threadIdx.x == 0) {
     mbar_init(bar, 1);
     fence_mbar_init();
   }
@@ -599,26 +655,50 @@ __global__ void __launch_bounds__(kTopoThreads, 1) topo_kernel(TopoParams p, Top
     if (threadIdx.x == 0) s_skip = (*reinterpret_cast<volatile int*>(queue) >= fr.n_lines) ? 1 : 0;
     __syncthreads();
     if (s_skip) continue;
-    // resident sources: the frame's first fr.resident charges (all of them, or
-    // a prefix of whole Kahan runs when the frame exceeds shared memory)
-    const int res = CAN_RESIDE ? fr.resident : 0;
-    if (res > 0) {
-      if (threadIdx.x == 0) {
-        const uint32_t blk = static_cast<uint32_t>(res / 2) * 16u;  // bytes of one block's prefix
-        const int n_blk = DIP ? 3 : 2;
-        mbar_arrive_expect_tx(bar, blk * n_blk);
-        const char* src = static_cast<const char*>(p.packed) + fr.packed_off * 16;
-        constexpr uint32_t kChunk = 32768;
-        for (int b = 0; b < n_blk; ++b) {  // block b of the frame starts at b * n_pad/2 pairs
-          const char* bs = src + static_cast<size_t>(b) * (fr.n_pad / 2) * 16;
-          char* bd = reinterpret_cast<char*>(sm_ch) + static_cast<size_t>(b) * blk;
-          for (uint32_t off = 0; off < blk; off += kChunk)
-            bulk_g2s(bd + off, bs + off, min(kChunk, blk - off), bar);
+    // sources in shared memory.  kResAny: the frame's first fr.resident
+    // sources -- all of them, or a prefix of whole Kahan runs when the frame
+    // exceeds shared memory -- copied block by block.  Otherwise whole frames
+    // (the host launches kResWhole only when every resident frame is entirely
+    // so) in one contiguous copy of the packed blocks: written as the
+    // block-wise copy, that kernel was compiled to a schedule 6% slower on
+    // the 8,000-charge workload.
+    int res = 0;
+    bool resident = false;
+    if constexpr (RES == kResAny) {
+      res = fr.resident;
+      if (res > 0) {
+        if (threadIdx.x == 0) {
+          const uint32_t blk = static_cast<uint32_t>(res / 2) * 16u;  // bytes of one block's prefix
+          const int n_blk = DIP ? 3 : 2;
+          mbar_arrive_expect_tx(bar, blk * n_blk);
+          const char* src = static_cast<const char*>(p.packed) + fr.packed_off * 16;
+          constexpr uint32_t kChunk = 32768;
+          for (int b = 0; b < n_blk; ++b) {  // block b of the frame starts at b * n_pad/2 pairs
+            const char* bs = src + static_cast<size_t>(b) * (fr.n_pad / 2) * 16;
+            char* bd = reinterpret_cast<char*>(sm_ch) + static_cast<size_t>(b) * blk;
+            for (uint32_t off = 0; off < blk; off += kChunk)
+              bulk_g2s(bd + off, bs + off, min(kChunk, blk - off), bar);
+          }
         }
+        const bool mine = mbar_wait(bar, load_parity, p.status);
+        load_parity ^= 1u;
+        if (!__syncthreads_and(mine)) return;
       }
-      const bool mine = mbar_wait(bar, load_parity, p.status);
-      load_parity ^= 1u;
-      if (!__syncthreads_and(mine)) return;
+    } else {
+      resident = RES == kResWhole && fr.resident;
+      if (resident) {
+        if (threadIdx.x == 0) {
+          const uint32_t total = static_cast<uint32_t>(fr.n_pad) * (DIP ? 24u : 16u);
+          mbar_arrive_expect_tx(bar, total);
+          const char* src = static_cast<const char*>(p.packed) + fr.packed_off * 16;
+          constexpr uint32_t kChunk = 32768;
+          for (uint32_t off = 0; off < total; off += kChunk)
+            bulk_g2s(reinterpret_cast<char*>(sm_ch) + off, src + off, min(kChunk, total - off), bar);
+        }
+        const bool mine = mbar_wait(bar, load_parity, p.status);
+        load_parity ^= 1u;
+        if (!__syncthreads_and(mine)) return;
+      }
     }
     FrameCtx fc;
     fc.line_off = fr.line_off;
@@ -634,9 +714,15 @@ __global__ void __launch_bounds__(kTopoThreads, 1) topo_kernel(TopoParams p, Top
         static_cast<const char*>(p.packed) + fr.packed_off * elem);
     const ulonglong2* gB = gA + fr.n_pad / 2;
     const ulonglong2* gC = DIP ? gA + fr.n_pad : nullptr;
-    const ulonglong2* sC = DIP ? sm_ch + res : nullptr;
-    run_frame<PREC, S, DIP>(p, fc, queue, gA, gB, gC, sm_ch, sm_ch + res / 2, sC, res / 2, fr.n_pad,
-                            my_rec, lane);
+    if constexpr (RES == kResAny) {
+      const ulonglong2* sC = DIP ? sm_ch + res : nullptr;
+      run_frame<PREC, S, DIP, RES>(p, fc, queue, gA, gB, gC, sm_ch, sm_ch + res / 2, sC, false,
+                                   res / 2, fr.n_pad, my_rec, lane);
+    } else {
+      const ulonglong2* sC = DIP ? sm_ch + fr.n_pad : nullptr;
+      run_frame<PREC, S, DIP, RES>(p, fc, queue, gA, gB, gC, sm_ch, sm_ch + fr.n_pad / 2, sC, resident,
+                                   0, fr.n_pad, my_rec, lane);
+    }
   }
 }
 
@@ -878,10 +964,10 @@ __global__ void __launch_bounds__(kEngineThreads, 2) engine_kernel(EngineParams 
         float total;
         const int n_pairs = n_pad / 2;
         switch (na) {
-          case 1: sweep_f32x2<1, S>(gA, gB, nullptr, 0, gA, gB, nullptr, n_pairs, lane, ex2, total); break;
-          case 2: sweep_f32x2<2, S>(gA, gB, nullptr, 0, gA, gB, nullptr, n_pairs, lane, ex2, total); break;
-          case 3: sweep_f32x2<(S > 2 ? 3 : 2), S>(gA, gB, nullptr, 0, gA, gB, nullptr, n_pairs, lane, ex2, total); break;
-          default: sweep_f32x2<S, S>(gA, gB, nullptr, 0, gA, gB, nullptr, n_pairs, lane, ex2, total); break;
+          case 1: sweep_f32x2<1, S>(nullptr, nullptr, nullptr, 0, gA, gB, nullptr, n_pairs, lane, ex2, total); break;
+          case 2: sweep_f32x2<2, S>(nullptr, nullptr, nullptr, 0, gA, gB, nullptr, n_pairs, lane, ex2, total); break;
+          case 3: sweep_f32x2<(S > 2 ? 3 : 2), S>(nullptr, nullptr, nullptr, 0, gA, gB, nullptr, n_pairs, lane, ex2, total); break;
+          default: sweep_f32x2<S, S>(nullptr, nullptr, nullptr, 0, gA, gB, nullptr, n_pairs, lane, ex2, total); break;
         }
         float Ef[3];
         const int rk = my_rank >= 0 ? my_rank : 0;
@@ -1016,22 +1102,22 @@ size_t topo_smem_bytes(int S, int max_resident_pad, bool dip = false) {
          static_cast<size_t>(max_resident_pad) * (dip ? 24 : 16);
 }
 
-template <int PREC, bool CAN_RESIDE, int S, bool DIP>
+template <int PREC, int RES, int S, bool DIP>
 cudaError_t launch_topo_t(const TopoParams& p, const TopoFrame& f0, int total_lines, int num_sms,
                           cudaStream_t s) {
-  const size_t smem = topo_smem_bytes(S, CAN_RESIDE ? p.max_resident_pad : 0, DIP);
-  cudaError_t err = cudaFuncSetAttribute(topo_kernel<PREC, CAN_RESIDE, S, DIP>,
+  const size_t smem = topo_smem_bytes(S, RES != kResNone ? p.max_resident_pad : 0, DIP);
+  cudaError_t err = cudaFuncSetAttribute(topo_kernel<PREC, RES, S, DIP>,
                                          cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          static_cast<int>(smem));
   if (err != cudaSuccess) return err;
   int per_sm = 1;
-  err = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, topo_kernel<PREC, CAN_RESIDE, S, DIP>,
+  err = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, topo_kernel<PREC, RES, S, DIP>,
                                                       kTopoThreads, smem);
   if (err != cudaSuccess) return err;
   per_sm = std::max(per_sm, 1);
   const int max_useful = (total_lines + kTopoWarps * S - 1) / (kTopoWarps * S);
   const int grid = std::max(1, std::min(num_sms * per_sm, max_useful));
-  topo_kernel<PREC, CAN_RESIDE, S, DIP><<<grid, kTopoThreads, smem, s>>>(p, f0);
+  topo_kernel<PREC, RES, S, DIP><<<grid, kTopoThreads, smem, s>>>(p, f0);
   return cudaGetLastError();
 }
 
@@ -1170,11 +1256,21 @@ cudaError_t launch_pack_topo_frames(int prec, int n_frames, const TopoFrame* d_f
   return cudaGetLastError();
 }
 
-template <int PREC, bool CAN_RESIDE, bool DIP = false>
+template <int PREC, int RES, bool DIP = false>
 cudaError_t launch_topo_s(const TopoParams& p, const TopoFrame& f0, int total_lines, int num_sms,
                           cudaStream_t s, int slots) {
-  return slots == 2 ? launch_topo_t<PREC, CAN_RESIDE, 2, DIP>(p, f0, total_lines, num_sms, s)
-                    : launch_topo_t<PREC, CAN_RESIDE, 4, DIP>(p, f0, total_lines, num_sms, s);
+  return slots == 2 ? launch_topo_t<PREC, RES, 2, DIP>(p, f0, total_lines, num_sms, s)
+                    : launch_topo_t<PREC, RES, 4, DIP>(p, f0, total_lines, num_sms, s);
+}
+
+// FP32C launch by residency mode; FP64 frames are never resident.
+template <bool DIP>
+cudaError_t launch_topo_mode(int prec, int mode, const TopoParams& p, const TopoFrame& f0,
+                             int num_sms, cudaStream_t s, int slots) {
+  if (prec == kFP64) return launch_topo_s<kFP64, kResNone, DIP>(p, f0, p.n_lines, num_sms, s, slots);
+  if (mode == kResWhole) return launch_topo_s<kFP32C, kResWhole, DIP>(p, f0, p.n_lines, num_sms, s, slots);
+  if (mode == kResAny) return launch_topo_s<kFP32C, kResAny, DIP>(p, f0, p.n_lines, num_sms, s, slots);
+  return launch_topo_s<kFP32C, kResNone, DIP>(p, f0, p.n_lines, num_sms, s, slots);
 }
 
 // Single frame: p.packed holds round_up(n_charges, topo_charge_pad(prec)) charges
@@ -1188,7 +1284,6 @@ cudaError_t launch_topo(int prec, const TopoParams& p_in, int num_sms, cudaStrea
   f0.line_off = 0;
   f0.n_pad = ((std::max(p.n_charges, 1) + pad - 1) / pad) * pad;
   f0.n_lines = p.n_lines;
-  const bool dip = p.source == kDipoles;
   f0.resident = topo_resident_count(prec, p.source, f0.n_pad);
   f0.pad_ = 0;
   f0.step = p.step;
@@ -1197,24 +1292,18 @@ cudaError_t launch_topo(int prec, const TopoParams& p_in, int num_sms, cudaStrea
   p.n_frames = 1;
   p.max_resident_pad = f0.resident;
   const int slots = tuned_topo_slots(prec, f0.resident == f0.n_pad, p.n_lines);
-  if (dip) {
-    if (prec == kFP64) return launch_topo_s<kFP64, false, true>(p, f0, p.n_lines, num_sms, s, slots);
-    if (f0.resident > 0) return launch_topo_s<kFP32C, true, true>(p, f0, p.n_lines, num_sms, s, slots);
-    return launch_topo_s<kFP32C, false, true>(p, f0, p.n_lines, num_sms, s, slots);
-  }
-  if (prec == kFP64) return launch_topo_s<kFP64, false>(p, f0, p.n_lines, num_sms, s, slots);
-  if (f0.resident > 0) return launch_topo_s<kFP32C, true>(p, f0, p.n_lines, num_sms, s, slots);
-  return launch_topo_s<kFP32C, false>(p, f0, p.n_lines, num_sms, s, slots);
+  const int mode = f0.resident == 0 ? kResNone : (f0.resident == f0.n_pad ? kResWhole : kResAny);
+  if (p.source == kDipoles) return launch_topo_mode<true>(prec, mode, p, f0, num_sms, s, slots);
+  return launch_topo_mode<false>(prec, mode, p, f0, num_sms, s, slots);
 }
 
 cudaError_t launch_topo_frames(int prec, const TopoParams& p, int num_sms, cudaStream_t s) {
   if (p.n_frames <= 0 || p.n_lines <= 0) return cudaSuccess;
   TopoFrame dummy{};
   const int slots = tuned_topo_slots(prec, p.all_resident != 0, p.n_lines);
-  if (prec == kFP64) return launch_topo_s<kFP64, false>(p, dummy, p.n_lines, num_sms, s, slots);
-  if (p.max_resident_pad > 0)
-    return launch_topo_s<kFP32C, true>(p, dummy, p.n_lines, num_sms, s, slots);
-  return launch_topo_s<kFP32C, false>(p, dummy, p.n_lines, num_sms, s, slots);
+  // kResWhole when no frame is partly resident (all_resident: every frame whole)
+  const int mode = p.max_resident_pad <= 0 ? kResNone : (p.all_resident ? kResWhole : kResAny);
+  return launch_topo_mode<false>(prec, mode, p, dummy, num_sms, s, slots);
 }
 
 }  // namespace cpetgb
