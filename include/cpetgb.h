@@ -144,7 +144,9 @@ int cpetgb_topo_batch(int precision, int mem, int n_frames, const int64_t* desc,
 /* Tile shapes are chosen per (operation, precision, class, size bucket):
  *   op 0 = grid sums: class = CPETGB_FIELD / CPETGB_ESP, size = pair evaluations
  *          of the launch (buckets of x4 from 1e6); variants 0..9 = points per
- *          thread {4, 8} x work items per SM {4, 8, 16, 32, 64} (default 1);
+ *          thread {4, 8} x work items per SM {4, 8, 16, 32, 64} (v / 5, v % 5),
+ *          10..13 = points per thread {4, 8} x {128, 256} items per SM
+ *          ((v - 10) / 2, (v - 10) % 2) (default 1);
  *   op 1 = streamlines: class = 1 if the frame's charges stay in shared memory,
  *          size = lines (buckets of x4 from 1e3); variants 0..1 = line slots per
  *          warp {4, 2} (default 0).

@@ -3,7 +3,8 @@
 The library picks a kernel variant per (operation, precision, class, size
 bucket) from a table (see ``cpetgb_tune_*`` in include/cpetgb.h):
 
-* grid sums (op 0): points per thread {4, 8} x work items per SM {4, 8, 16, 32, 64};
+* grid sums (op 0): points per thread {4, 8} x work items per SM {4, 8, 16, 32, 64}
+  (variants 0-9) and {128, 256} (variants 10-13);
   class = field / potential; size = pair evaluations of the launch;
 * streamlines (op 1): line slots per warp {4, 2}; class = charges resident
   in shared memory or streamed from L2; size = number of lines.

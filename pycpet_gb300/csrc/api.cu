@@ -169,7 +169,9 @@ std::mutex g_tune_mu;
 std::map<int, int> g_tune;
 
 constexpr int kOpGrid = 0, kOpTopo = 1;
-constexpr int kGridVariants = 10;  // points per thread {4, 8} x work items per SM {4, 8, 16, 32, 64}
+// points per thread {4, 8} x work items per SM: variants 0-9 {4, 8, 16, 32, 64},
+// 10-13 {128, 256} (numbered after the first ten so saved tables keep their meaning)
+constexpr int kGridVariants = 14;
 constexpr int kTopoVariants = 2;  // line slots per warp {4, 2}
 
 int size_bucket(double v, double base) {
@@ -962,6 +964,11 @@ int cpetgb::tuned_topo_slots(int prec, bool resident, int n_lines) {
 void cpetgb::tuned_grid_shape(int prec, int kind, double pair_evals, int* ppt, int* items_per_sm) {
   int v = tune_choose(tune_key(kOpGrid, prec, kind, pair_evals));
   if (v < 0 || v >= kGridVariants) v = 1;  // untuned: 4 points per thread, 8 items per SM
+  if (v >= 10) {
+    *ppt = ((v - 10) / 2) == 1 ? 8 : 4;
+    *items_per_sm = ((v - 10) % 2) == 0 ? 128 : 256;
+    return;
+  }
   static const int ips[5] = {4, 8, 16, 32, 64};
   *ppt = (v / 5) == 1 ? 8 : 4;
   *items_per_sm = ips[v % 5];

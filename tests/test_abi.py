@@ -105,13 +105,13 @@ def test_tuning_table_round_trip(built):
     from pycpet_gb300 import _lib
 
     L = _lib.lib()
-    assert L.cpetgb_tune_variants(0) == 10 and L.cpetgb_tune_variants(1) == 2
+    assert L.cpetgb_tune_variants(0) == 14 and L.cpetgb_tune_variants(1) == 2
     k_small = L.cpetgb_tune_key(0, 1, 0, 1e5)
     k_big = L.cpetgb_tune_key(0, 1, 0, 1e10)
     assert k_small >= 0 and k_big > k_small
     assert L.cpetgb_tune_get(k_big) == -1
     assert L.cpetgb_tune_set(k_big, 4) == 0 and L.cpetgb_tune_get(k_big) == 4
-    assert L.cpetgb_tune_set(k_big, 10) == _lib.EINVAL      # no such variant
+    assert L.cpetgb_tune_set(k_big, 14) == _lib.EINVAL      # no such variant
     assert L.cpetgb_tune_set(k_big, -1) == 0 and L.cpetgb_tune_get(k_big) == -1
     kt = L.cpetgb_tune_key(1, 1, 1, 1e5)
     assert L.cpetgb_tune_set(kt, 2) == _lib.EINVAL and L.cpetgb_tune_set(kt, 1) == 0
