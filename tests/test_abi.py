@@ -117,3 +117,26 @@ def test_tuning_table_round_trip(built):
     assert L.cpetgb_tune_set(kt, 2) == _lib.EINVAL and L.cpetgb_tune_set(kt, 1) == 0
     assert L.cpetgb_tune_set(kt, -1) == 0
     assert L.cpetgb_tune_key(7, 1, 0, 1.0) == _lib.EINVAL
+
+
+def test_shipped_tuning_table_is_valid(built):
+    """Every entry of the shipped GB300 table names an existing variant of a
+    valid key (grid keys: op 0; streamline keys: op 1)."""
+    import json
+    import os
+
+    from conftest import ROOT
+    from pycpet_gb300 import _lib
+
+    L = _lib.lib()
+    with open(os.path.join(ROOT, "pycpet_gb300", "tuned", "nvidia_gb300.json")) as fh:
+        table = json.load(fh)["table"]
+    assert table
+    for k, v in table.items():
+        op = int(k) >> 12
+        assert op in (0, 1)
+        assert 0 <= v < L.cpetgb_tune_variants(op), (k, v)
+        before = L.cpetgb_tune_get(int(k))  # restored: the table is process state
+        assert L.cpetgb_tune_set(int(k), v) == 0
+        assert L.cpetgb_tune_get(int(k)) == v
+        assert L.cpetgb_tune_set(int(k), before) == 0
