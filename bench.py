@@ -351,18 +351,9 @@ def main():
 def grid_frames(n_frames, seed=2024):
     """Batched volume workload: N ~ U[3,000, 40,000] charges (cube edge scaled
     to keep the density), grids of 11^3, 21^3 or 31^3 points at 0.1 A."""
-    from pycpet_gb300.synth import make_frame
+    from pycpet_gb300.synth import volume_batch_frames
 
-    rng = np.random.default_rng(seed)
-    frames = []
-    for f in range(n_frames):
-        n = int(rng.integers(3000, 40001))
-        half = float(rng.choice([0.5, 1.0, 1.5]))
-        g = np.linspace(-half, half, int(round(2 * half / 0.1)) + 1)
-        pts = np.stack(np.meshgrid(g, g, g, indexing="ij"), -1).reshape(-1, 3)
-        fr = make_frame(n, seed=5000 + f)
-        frames.append((pts, fr["x"], fr["q"]))
-    return frames
+    return volume_batch_frames(n_frames, seed)
 
 
 def grid_main(args, rank, world, dev, torch, dist):

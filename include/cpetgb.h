@@ -21,7 +21,10 @@
  *   - Precision: CPETGB_FP64 = every operation in IEEE double (the plain
  *     drop-in); CPETGB_FP32C = FP32 pair terms with compensated (Kahan)
  *     accumulation across charge tiles, FP64 for streamline positions and the
- *     final curvature / distance.
+ *     final curvature / distance.  FP32C fields are refined: the points where
+ *     |E| is below a fraction (cpetgb_set_field_refinement, default 0.1) of
+ *     their frame's median |E| -- where the pair terms cancel and FP32
+ *     rounding is largest relative to |E| -- are recomputed in IEEE double.
  */
 #ifndef CPETGB_H
 #define CPETGB_H
@@ -59,9 +62,18 @@ int cpetgb_last_error(char* buf, size_t len);
 int cpetgb_device_sms(void);
 /* Waits for `stream` and returns (then clears) the device-side status. */
 int cpetgb_synchronize(void* stream);
-/* Precision used by the float32 drop-in entry points below (default FP32C). */
+/* Precision used by the float32 drop-in entry points below (default FP32C).
+ * Process-wide; the *_p variants take the precision per call instead. */
 int cpetgb_set_default_precision(int precision);
 int cpetgb_get_default_precision(void);
+/* FP32C field refinement threshold tau in [0, 1] (0 = off; default 0.1):
+ * after the FP32C pass, every point of a frame with |E| < tau * (the frame's
+ * median |E|, rounded down to 1/16 octave) is recomputed in IEEE double over
+ * all of the frame's charges.  Process-wide setting read when a call (or a
+ * plan, at creation) is made.  No counterpart in the reference, whose field is
+ * plain float (CPET/utils/math_module.c:405-451). */
+int cpetgb_set_field_refinement(double tau);
+double cpetgb_field_refinement(void);
 
 /* Pipe throughput microbenchmark on the current device (roofline denominators):
  * kind 0 FP32 FFMA flop/s, 1 FP64 DFMA flop/s, 2 MUFU rsqrt op/s, 3 FP32x2 FFMA2 flop/s,
@@ -100,6 +112,28 @@ int cpetgb_thread_operation_batch(int n_lines, int n_charges, const int32_t* n_i
  * call: ESP[p] = k sum q / |x_0[p] - x|. */
 int cpetgb_compute_esp_grid(int total_points, int n_charges, const float* x_0, const float* x,
                             const float* Q, float* ESP);
+
+/* The same seven calls with the precision passed per call (CPETGB_FP64 or
+ * CPETGB_FP32C) instead of read from the library default: callers that mix
+ * precisions from several threads use these.  Arguments otherwise as above. */
+int cpetgb_compute_looped_field_p(int precision, int total_points, int n_charges,
+                                  const float* x_0, const float* x, const float* Q, float* E);
+int cpetgb_calc_esp_base_p(int precision, float* ESP, const float* x_init, int n_charges,
+                           const float* x, const float* Q);
+int cpetgb_calc_field_p(int precision, float* E, const float* x_init, int n_charges,
+                        const float* x, const float* Q);
+int cpetgb_thread_operation_p(int precision, int n_charges, int n_iter, float step_size,
+                              const float* x_0, const float* dimensions, const float* x,
+                              const float* Q, float* ret);
+int cpetgb_thread_operation_dipole_p(int precision, int n_dipoles, int n_iter, float step_size,
+                                     const float* x_0, const float* dimensions, const float* x,
+                                     const float* mu, float* ret);
+int cpetgb_thread_operation_batch_p(int precision, int n_lines, int n_charges,
+                                    const int32_t* n_iter, float step_size, const float* x_0,
+                                    const float* dimensions, const float* x, const float* Q,
+                                    float* ret);
+int cpetgb_compute_esp_grid_p(int precision, int total_points, int n_charges, const float* x_0,
+                              const float* x, const float* Q, float* ESP);
 
 /* ---- general entry points (double buffers, host or device) --------------- */
 /* Field at n_points points: points[P][3], x[N][3], q[N] -> field[P][3].

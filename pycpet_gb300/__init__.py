@@ -6,7 +6,7 @@ this package is the host side: ctypes binding (``_lib``), array-level API
 math functions of ``CPET.utils.calculator`` (``calculator``) and the
 calculator hot-path methods (``drop_in``).
 """
-from ._lib import CpetgbError  # noqa: F401
+from ._lib import CpetgbError, set_field_refinement  # noqa: F401
 from .core import (GridBatch, TopoBatch, chi2_distance_matrix, esp_grid, field_distance_matrix,  # noqa: F401
                    field_grid, point_field, synchronize, topo_dipole_lines, topo_hist2d, topo_hist2d_sets,
                    topo_lines)

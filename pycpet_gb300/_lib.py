@@ -45,6 +45,14 @@ SIGNATURES = {
     "cpetgb_thread_operation_batch": [_i, _i, _vp, _f, _vp, _vp, _vp, _vp, _vp],
     "cpetgb_thread_operation_dipole": [_i, _i, _f, _vp, _vp, _vp, _vp, _vp],
     "cpetgb_compute_esp_grid": [_i, _i, _vp, _vp, _vp, _vp],
+    "cpetgb_compute_looped_field_p": [_i, _i, _i, _vp, _vp, _vp, _vp],
+    "cpetgb_calc_esp_base_p": [_i, _vp, _vp, _i, _vp, _vp],
+    "cpetgb_calc_field_p": [_i, _vp, _vp, _i, _vp, _vp],
+    "cpetgb_thread_operation_p": [_i, _i, _i, _f, _vp, _vp, _vp, _vp, _vp],
+    "cpetgb_thread_operation_batch_p": [_i, _i, _i, _vp, _f, _vp, _vp, _vp, _vp, _vp],
+    "cpetgb_thread_operation_dipole_p": [_i, _i, _i, _f, _vp, _vp, _vp, _vp, _vp],
+    "cpetgb_compute_esp_grid_p": [_i, _i, _i, _vp, _vp, _vp, _vp],
+    "cpetgb_set_field_refinement": [_d],
     "cpetgb_field_grid": [_i, _i, _i, _i, _vp, _vp, _vp, _i, _vp, _vp],
     "cpetgb_esp_grid": [_i, _i, _i, _i, _vp, _vp, _vp, _vp, _vp],
     "cpetgb_grid_batch": [_i, _i, _i, _i, _i, _vp, _vp, _vp, _vp, _vp, _vp],
@@ -98,6 +106,8 @@ def lib(path: str | None = None):
         fn = getattr(L, name)
         fn.argtypes = argtypes
         fn.restype = ctypes.c_int
+    L.cpetgb_field_refinement.argtypes = []
+    L.cpetgb_field_refinement.restype = ctypes.c_double
     _lib, _path = L, so
     _load_tuned_table()
     return L
@@ -135,6 +145,13 @@ def measure_peak(kind: int) -> float:
     v = ctypes.c_double(0.0)
     check(lib().cpetgb_measure_peak(kind, ctypes.byref(v)))
     return v.value
+
+
+def set_field_refinement(tau: float) -> float:
+    """Sets the FP32C field refinement threshold (0 = off) and returns the old one."""
+    old = lib().cpetgb_field_refinement()
+    check(lib().cpetgb_set_field_refinement(float(tau)))
+    return old
 
 
 def device_sms() -> int:

@@ -35,34 +35,36 @@ _i1 = npct.ndpointer(dtype=np.int32, ndim=1, flags="C")
 
 
 class Math_ops:
+    """``precision`` (``"fp32c"`` / ``"fp64"``, default: the library default)
+    travels with every call (the ``*_p`` entry points), so objects of different
+    precisions can be used from several threads at once."""
+
     def __init__(self, shared_loc=None, precision=None):
         # shared_loc names the GPU library (default: the in-tree libcpetgb.so)
         self.math = _lib.lib(shared_loc)
         self.precision = None if precision is None else precision_code(precision)
         # typed views with the reference's ndpointer checks (c_ops.py:85-138)
         L = ctypes.CDLL(self.math._name)
-        self._thread_op = L.cpetgb_thread_operation
-        self._thread_op.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_float, _f1, _f1, _f2, _f1, _f1]
-        self._thread_op.restype = ctypes.c_int
-        self._esp_base = L.cpetgb_calc_esp_base
-        self._esp_base.argtypes = [_f1, _f1, ctypes.c_int, _f2, _f1]
-        self._esp_base.restype = ctypes.c_int
-        self._calc_field = L.cpetgb_calc_field
-        self._calc_field.argtypes = [_f1, _f1, ctypes.c_int, _f2, _f1]
-        self._calc_field.restype = ctypes.c_int
-        self._thread_op_dipole = L.cpetgb_thread_operation_dipole
-        self._thread_op_dipole.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_float, _f1, _f1, _f2, _f2, _f1]
-        self._thread_op_dipole.restype = ctypes.c_int
+        _c = ctypes.c_int
 
-    def _with_precision(self, fn, *args):
-        if self.precision is None:
-            return _lib.check(fn(*args))
-        old = self.math.cpetgb_get_default_precision()
-        _lib.check(self.math.cpetgb_set_default_precision(self.precision))
-        try:
-            return _lib.check(fn(*args))
-        finally:
-            self.math.cpetgb_set_default_precision(old)
+        def typed(name, argtypes):
+            fn = getattr(L, name)
+            fn.argtypes = [_c] + argtypes
+            fn.restype = ctypes.c_int
+            return fn
+
+        self._thread_op = typed("cpetgb_thread_operation_p",
+                                [_c, _c, ctypes.c_float, _f1, _f1, _f2, _f1, _f1])
+        self._esp_base = typed("cpetgb_calc_esp_base_p", [_f1, _f1, _c, _f2, _f1])
+        self._calc_field = typed("cpetgb_calc_field_p", [_f1, _f1, _c, _f2, _f1])
+        self._thread_op_dipole = typed("cpetgb_thread_operation_dipole_p",
+                                       [_c, _c, ctypes.c_float, _f1, _f1, _f2, _f2, _f1])
+
+    def _prec(self) -> int:
+        return self.math.cpetgb_get_default_precision() if self.precision is None else self.precision
+
+    def _call(self, fn, *args):
+        return _lib.check(fn(self._prec(), *args))
 
     def compute_looped_field(self, x_0, x, Q):
         res = np.zeros_like(x_0, dtype="float32")
@@ -71,8 +73,8 @@ class Math_ops:
         xx = np.ascontiguousarray(np.array(x, dtype="float32"))
         qq = np.ascontiguousarray(np.array(Q, dtype="float32"))
         res = np.ascontiguousarray(res)
-        self._with_precision(self.math.cpetgb_compute_looped_field, int(x0.shape[0]), len(qq),
-                             x0.ctypes.data, xx.ctypes.data, qq.ctypes.data, res.ctypes.data)
+        self._call(self.math.cpetgb_compute_looped_field_p, int(x0.shape[0]), len(qq),
+                   x0.ctypes.data, xx.ctypes.data, qq.ctypes.data, res.ctypes.data)
         return res
 
     def compute_esp_grid(self, x_0, x, Q):
@@ -80,21 +82,21 @@ class Math_ops:
         xx = np.ascontiguousarray(np.array(x, dtype="float32")).reshape(-1, 3)
         qq = np.ascontiguousarray(np.array(Q, dtype="float32")).reshape(-1)
         res = np.zeros(x0.shape[0], dtype="float32")
-        self._with_precision(self.math.cpetgb_compute_esp_grid, x0.shape[0], len(qq), x0.ctypes.data,
-                             xx.ctypes.data, qq.ctypes.data, res.ctypes.data)
+        self._call(self.math.cpetgb_compute_esp_grid_p, x0.shape[0], len(qq), x0.ctypes.data,
+                   xx.ctypes.data, qq.ctypes.data, res.ctypes.data)
         return res
 
     def thread_operation(self, x_0, n_iter, x, Q, step_size, dimensions):
         res = np.zeros(2, dtype="float32")
         n_charges = len(Q)
         Q = Q.reshape(-1)
-        self._with_precision(self._thread_op, n_charges, int(n_iter), step_size, x_0, dimensions, x, Q, res)
+        self._call(self._thread_op, n_charges, int(n_iter), step_size, x_0, dimensions, x, Q, res)
         return res
 
     def thread_operation_dipole(self, x_0, n_iter, x, mu, step_size, dimensions):
         """One streamline through point dipoles (c_ops.py:304-325): res = (dist, curv)."""
         res = np.zeros(2, dtype="float32")
-        self._with_precision(self._thread_op_dipole, len(mu), int(n_iter), step_size, x_0, dimensions, x, mu, res)
+        self._call(self._thread_op_dipole, len(mu), int(n_iter), step_size, x_0, dimensions, x, mu, res)
         return res
 
     def thread_operation_batch(self, x_0, n_iter, x, Q, step_size, dimensions):
@@ -104,22 +106,22 @@ class Math_ops:
         qq = np.ascontiguousarray(np.array(Q, dtype="float32")).reshape(-1)
         dims = np.ascontiguousarray(np.array(dimensions, dtype="float32")).reshape(3)
         res = np.zeros((x0.shape[0], 2), dtype="float32")
-        self._with_precision(self.math.cpetgb_thread_operation_batch, x0.shape[0], len(qq), it.ctypes.data,
-                             float(step_size), x0.ctypes.data, dims.ctypes.data, xx.ctypes.data, qq.ctypes.data,
-                             res.ctypes.data)
+        self._call(self.math.cpetgb_thread_operation_batch_p, x0.shape[0], len(qq), it.ctypes.data,
+                   float(step_size), x0.ctypes.data, dims.ctypes.data, xx.ctypes.data, qq.ctypes.data,
+                   res.ctypes.data)
         return res
 
     def calc_esp_base(self, x_0, x, Q):
         res = np.zeros(1, dtype="float32")
-        self._with_precision(self._esp_base, res, x_0, len(Q), x, Q.reshape(len(Q)))
+        self._call(self._esp_base, res, x_0, len(Q), x, Q.reshape(len(Q)))
         return res
 
     def calc_field_base(self, x_0, x, Q):
         res = np.zeros(3, dtype="float32")
-        self._with_precision(self._calc_field, res, x_0, len(Q), x, Q.reshape(len(Q)))
+        self._call(self._calc_field, res, x_0, len(Q), x, Q.reshape(len(Q)))
         return res
 
     def calc_field(self, x_0, x, Q):
         res = np.zeros(3, dtype="float32")
-        self._with_precision(self._calc_field, res, x_0, len(Q), x, Q.reshape(len(Q)))
+        self._call(self._calc_field, res, x_0, len(Q), x, Q.reshape(len(Q)))
         return res

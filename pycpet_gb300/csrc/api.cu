@@ -31,6 +31,9 @@ constexpr int kMaxDevices = 64;
 thread_local std::string g_err;
 std::mutex g_mu;
 std::atomic<int> g_default_prec{CPETGB_FP32C};
+// FP32C field: points with |E| below this fraction of their frame's median |E|
+// are recomputed in IEEE double (0 turns the refinement off).
+std::atomic<double> g_refine_tau{0.1};
 
 struct Ctx {
   bool ready = false;
@@ -211,20 +214,26 @@ int tune_choose(int key) {
 
 void plan_grid(int n_frames, const int64_t* desc, int sms, GridPlan& plan, int ppt,
                int items_per_sm) {
-  double total = 0.0;
-  for (int f = 0; f < n_frames; ++f) total += double(desc[4 * f + 1]) * double(desc[4 * f + 3]);
   const int tile = kGridThreads * ppt;
-  // about items_per_sm items per SM so the largest-first order balances the tail
+  // A CTA's time is proportional to its charge count alone: every thread
+  // evaluates all of its point slots, valid or not.  Each frame's points are
+  // cut into equal tiles, and charge ranges are split so that about
+  // items_per_sm items of equal cost fall on each SM.
+  auto n_tiles = [&](int64_t P) { return (P + tile - 1) / tile; };
+  double total = 0.0;
+  for (int f = 0; f < n_frames; ++f)
+    total += double(n_tiles(desc[4 * f + 3])) * tile * double(desc[4 * f + 1]);
   const double target = std::max(1.0, total / (double(std::max(sms, 1)) * items_per_sm));
   for (int f = 0; f < n_frames; ++f) {
     const int64_t co = desc[4 * f + 0], n = desc[4 * f + 1];
     const int64_t po = desc[4 * f + 2], P = desc[4 * f + 3];
-    for (int64_t pb = 0; pb < P; pb += tile) {
-      const int pc = static_cast<int>(std::min<int64_t>(tile, P - pb));
+    const int64_t nt = n_tiles(P);
+    for (int64_t ti = 0; ti < nt; ++ti) {
+      const int64_t pb = ti * (P / nt) + std::min<int64_t>(ti, P % nt);
+      const int pc = static_cast<int>(P / nt + (ti < P % nt ? 1 : 0));
       int64_t split = 1;
       if (n > 0) {
-        const double cost = double(pc) * double(n);
-        split = static_cast<int64_t>(std::ceil(cost / target));
+        split = static_cast<int64_t>(std::ceil(double(tile) * double(n) / target));
         split = std::max<int64_t>(1, std::min<int64_t>(split, std::max<int64_t>(1, n / 256)));
       }
       const int64_t chunk = n > 0 ? (n + split - 1) / split : 0;
@@ -249,9 +258,17 @@ void plan_grid(int n_frames, const int64_t* desc, int sms, GridPlan& plan, int p
       }
     }
   }
-  std::stable_sort(plan.items.begin(), plan.items.end(), [](const GridItem& a, const GridItem& b) {
-    return int64_t(a.p_count) * a.n_count > int64_t(b.p_count) * b.n_count;
-  });
+  // longest first, so the last wave holds the shortest items
+  std::stable_sort(plan.items.begin(), plan.items.end(),
+                   [](const GridItem& a, const GridItem& b) { return a.n_count > b.n_count; });
+}
+
+// Entries the refinement list may need: every point of every frame (frames
+// may share point ranges, so this is the sum, not the extent).
+int64_t refine_list_len(int n_frames, const int64_t* desc) {
+  int64_t n = 0;
+  for (int f = 0; f < n_frames; ++f) n += desc[4 * f + 3];
+  return std::max<int64_t>(n, 1);
 }
 
 double grid_pair_evals(int n_frames, const int64_t* desc) {
@@ -319,6 +336,17 @@ int grid_batch_impl(int kind, int prec, int mem, int clamp, int n_frames, const 
      "grid kernel launch");
   CK(launch_grid_final(kind, static_cast<int>(plan.finals.size()), d_fin, partial, dout, s),
      "grid reduction launch");
+  const double tau = g_refine_tau.load();
+  if (kind == CPETGB_FIELD && prec == CPETGB_FP32C && tau > 0.0 && tot_ch > 0) {
+    int64_t *d_desc = nullptr, *list = nullptr;
+    int* count = nullptr;
+    CK(h2d(&d_desc, S, desc, size_t(n_frames) * 4), "copy frame table");
+    CK(S.get(&list, size_t(refine_list_len(n_frames, desc)) * 2), "alloc refinement list");
+    CK(S.get(&count, 1), "alloc refinement count");
+    CK(launch_grid_refine(n_frames, d_desc, dp, dx, dq, dout, clamp ? 1 : 0, tau, list, count,
+                          c->sms, s),
+       "field refinement launch");
+  }
   if (mem == CPETGB_HOST) {
     CK(cudaMemcpyAsync(out, dout, size_t(tot_pts) * NC * sizeof(double), cudaMemcpyDeviceToHost, s),
        "copy output");
@@ -863,6 +891,22 @@ int grid_plan_impl(cpetgb_plan** out_plan, int kind, int prec, int clamp, int n_
     delete pl;
     return cuda_fail(e, "plan allocation");
   }
+  const double tau = g_refine_tau.load();
+  const bool refine = kind == CPETGB_FIELD && prec == CPETGB_FP32C && tau > 0.0 && tot_ch > 0;
+  int64_t *d_desc = nullptr, *list = nullptr;
+  int* count = nullptr;
+  if (refine) {
+    e = plan_alloc(pl->bufs, &d_desc, size_t(n_frames) * 4);
+    if (e == cudaSuccess)
+      e = cudaMemcpy(d_desc, desc, size_t(n_frames) * 4 * sizeof(int64_t), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = plan_alloc(pl->bufs, &list, size_t(refine_list_len(n_frames, desc)) * 2);
+    if (e == cudaSuccess) e = plan_alloc(pl->bufs, &count, 1);
+    if (e == cudaSuccess) e = preload_grid_refine();
+    if (e != cudaSuccess) {
+      delete pl;
+      return cuda_fail(e, "plan allocation");
+    }
+  }
   const int n_items = static_cast<int>(gp.items.size()), n_fin = static_cast<int>(gp.finals.size());
   e = preload_grid_kernels(prec, kind, clamp ? 1 : 0, ppt);
   if (e != cudaSuccess) {
@@ -875,6 +919,10 @@ int grid_plan_impl(cpetgb_plan** out_plan, int kind, int prec, int clamp, int n_
                    c->status, cs),
        "grid kernel launch");
     CK(launch_grid_final(kind, n_fin, d_fin, partial, out, cs), "grid reduction launch");
+    if (refine)
+      CK(launch_grid_refine(n_frames, d_desc, pts, x, q, out, clamp ? 1 : 0, tau, list, count,
+                            c->sms, cs),
+         "field refinement launch");
     return CPETGB_OK;
   });
   if (rc != CPETGB_OK) {
@@ -996,6 +1044,15 @@ int cpetgb_synchronize(void* stream) {
   if (!c) return rc;
   return finish(c, static_cast<cudaStream_t>(stream));
 }
+
+int cpetgb_set_field_refinement(double tau) {
+  if (!(tau >= 0.0) || !std::isfinite(tau) || tau > 1.0)
+    return fail(CPETGB_EINVAL, "refinement threshold must be in [0, 1], got %g", tau);
+  g_refine_tau.store(tau);
+  return CPETGB_OK;
+}
+
+double cpetgb_field_refinement(void) { return g_refine_tau.load(); }
 
 int cpetgb_set_default_precision(int precision) {
   if (!valid_prec(precision)) return fail(CPETGB_EINVAL, "bad precision %d", precision);
@@ -1149,8 +1206,8 @@ int cpetgb_field_distance_matrix(int precision, int mem, int n, int n_points,
 
 // ---- float32 drop-ins ----------------------------------------------------
 
-int cpetgb_compute_looped_field(int total_points, int n_charges, const float* x_0,
-                                const float* x, const float* Q, float* E) {
+int cpetgb_compute_looped_field_p(int precision, int total_points, int n_charges,
+                                  const float* x_0, const float* x, const float* Q, float* E) {
   if (total_points < 0 || n_charges < 0) return fail(CPETGB_EINVAL, "negative size");
   if (total_points == 0) return CPETGB_OK;
   if (!x_0 || !E || (n_charges && (!x || !Q))) return fail(CPETGB_EINVAL, "NULL pointer");
@@ -1158,15 +1215,15 @@ int cpetgb_compute_looped_field(int total_points, int n_charges, const float* x_
   auto xx = widen(x, size_t(n_charges) * 3);
   auto qq = widen(Q, size_t(n_charges));
   std::vector<double> out(size_t(total_points) * 3);
-  const int rc = cpetgb_field_grid(g_default_prec.load(), CPETGB_HOST, total_points, n_charges,
+  const int rc = cpetgb_field_grid(precision, CPETGB_HOST, total_points, n_charges,
                                    p.data(), xx.data(), qq.data(), 1, out.data(), nullptr);
   if (rc != CPETGB_OK) return rc;
   for (size_t i = 0; i < out.size(); ++i) E[i] = static_cast<float>(out[i]);
   return CPETGB_OK;
 }
 
-int cpetgb_compute_esp_grid(int total_points, int n_charges, const float* x_0, const float* x,
-                            const float* Q, float* ESP) {
+int cpetgb_compute_esp_grid_p(int precision, int total_points, int n_charges, const float* x_0,
+                              const float* x, const float* Q, float* ESP) {
   if (total_points < 0 || n_charges < 0) return fail(CPETGB_EINVAL, "negative size");
   if (total_points == 0) return CPETGB_OK;
   if (!x_0 || !ESP || (n_charges && (!x || !Q))) return fail(CPETGB_EINVAL, "NULL pointer");
@@ -1174,40 +1231,41 @@ int cpetgb_compute_esp_grid(int total_points, int n_charges, const float* x_0, c
   auto xx = widen(x, size_t(n_charges) * 3);
   auto qq = widen(Q, size_t(n_charges));
   std::vector<double> out(static_cast<size_t>(total_points));
-  const int rc = cpetgb_esp_grid(g_default_prec.load(), CPETGB_HOST, total_points, n_charges,
+  const int rc = cpetgb_esp_grid(precision, CPETGB_HOST, total_points, n_charges,
                                  p.data(), xx.data(), qq.data(), out.data(), nullptr);
   if (rc != CPETGB_OK) return rc;
   for (size_t i = 0; i < out.size(); ++i) ESP[i] = static_cast<float>(out[i]);
   return CPETGB_OK;
 }
 
-int cpetgb_calc_esp_base(float* ESP, const float* x_init, int n_charges, const float* x,
-                         const float* Q) {
+int cpetgb_calc_esp_base_p(int precision, float* ESP, const float* x_init, int n_charges,
+                           const float* x, const float* Q) {
   if (!ESP || !x_init) return fail(CPETGB_EINVAL, "NULL pointer");
   float v = 0.f;
-  const int rc = cpetgb_compute_esp_grid(1, n_charges, x_init, x, Q, &v);
+  const int rc = cpetgb_compute_esp_grid_p(precision, 1, n_charges, x_init, x, Q, &v);
   if (rc != CPETGB_OK) return rc;
   ESP[0] += v;
   return CPETGB_OK;
 }
 
-int cpetgb_calc_field(float* E, const float* x_init, int n_charges, const float* x,
-                      const float* Q) {
+int cpetgb_calc_field_p(int precision, float* E, const float* x_init, int n_charges,
+                        const float* x, const float* Q) {
   if (!E || !x_init) return fail(CPETGB_EINVAL, "NULL pointer");
   if (n_charges < 0) return fail(CPETGB_EINVAL, "negative size");
   double p[3] = {x_init[0], x_init[1], x_init[2]}, out[3];
   auto xx = widen(x, size_t(n_charges) * 3);
   auto qq = widen(Q, size_t(n_charges));
-  const int rc = cpetgb_field_grid(g_default_prec.load(), CPETGB_HOST, 1, n_charges, p, xx.data(),
+  const int rc = cpetgb_field_grid(precision, CPETGB_HOST, 1, n_charges, p, xx.data(),
                                    qq.data(), 0, out, nullptr);
   if (rc != CPETGB_OK) return rc;
   for (int k = 0; k < 3; ++k) E[k] = static_cast<float>(out[k]);
   return CPETGB_OK;
 }
 
-int cpetgb_thread_operation_batch(int n_lines, int n_charges, const int32_t* n_iter,
-                                  float step_size, const float* x_0, const float* dimensions,
-                                  const float* x, const float* Q, float* ret) {
+int cpetgb_thread_operation_batch_p(int precision, int n_lines, int n_charges,
+                                    const int32_t* n_iter, float step_size, const float* x_0,
+                                    const float* dimensions, const float* x, const float* Q,
+                                    float* ret) {
   if (n_lines < 0 || n_charges < 0) return fail(CPETGB_EINVAL, "negative size");
   if (n_lines == 0) return CPETGB_OK;
   if (!n_iter || !x_0 || !dimensions || !ret || (n_charges && (!x || !Q)))
@@ -1217,7 +1275,7 @@ int cpetgb_thread_operation_batch(int n_lines, int n_charges, const int32_t* n_i
   auto qq = widen(Q, size_t(n_charges));
   const double half[3] = {dimensions[0], dimensions[1], dimensions[2]};
   std::vector<double> res(size_t(n_lines) * 2);
-  const int rc = cpetgb_topo_lines(g_default_prec.load(), CPETGB_HOST, n_lines, n_charges,
+  const int rc = cpetgb_topo_lines(precision, CPETGB_HOST, n_lines, n_charges,
                                    s.data(), n_iter, double(step_size), half, xx.data(),
                                    qq.data(), res.data(), nullptr, nullptr, nullptr);
   if (rc != CPETGB_OK) return rc;
@@ -1225,16 +1283,17 @@ int cpetgb_thread_operation_batch(int n_lines, int n_charges, const int32_t* n_i
   return CPETGB_OK;
 }
 
-int cpetgb_thread_operation(int n_charges, int n_iter, float step_size, const float* x_0,
-                            const float* dimensions, const float* x, const float* Q,
-                            float* ret) {
+int cpetgb_thread_operation_p(int precision, int n_charges, int n_iter, float step_size,
+                              const float* x_0, const float* dimensions, const float* x,
+                              const float* Q, float* ret) {
   const int32_t it = n_iter;
-  return cpetgb_thread_operation_batch(1, n_charges, &it, step_size, x_0, dimensions, x, Q, ret);
+  return cpetgb_thread_operation_batch_p(precision, 1, n_charges, &it, step_size, x_0, dimensions,
+                                         x, Q, ret);
 }
 
-int cpetgb_thread_operation_dipole(int n_dipoles, int n_iter, float step_size, const float* x_0,
-                                   const float* dimensions, const float* x, const float* mu,
-                                   float* ret) {
+int cpetgb_thread_operation_dipole_p(int precision, int n_dipoles, int n_iter, float step_size,
+                                     const float* x_0, const float* dimensions, const float* x,
+                                     const float* mu, float* ret) {
   if (n_dipoles < 0) return fail(CPETGB_EINVAL, "negative size");
   if (!x_0 || !dimensions || !ret || (n_dipoles && (!x || !mu)))
     return fail(CPETGB_EINVAL, "NULL pointer");
@@ -1244,13 +1303,57 @@ int cpetgb_thread_operation_dipole(int n_dipoles, int n_iter, float step_size, c
   const double half[3] = {dimensions[0], dimensions[1], dimensions[2]};
   const int32_t it = n_iter;
   double res[2];
-  const int rc = cpetgb_topo_dipole_lines(g_default_prec.load(), CPETGB_HOST, 1, n_dipoles,
+  const int rc = cpetgb_topo_dipole_lines(precision, CPETGB_HOST, 1, n_dipoles,
                                           s.data(), &it, double(step_size), half, xx.data(),
                                           mm.data(), res, nullptr, nullptr, nullptr);
   if (rc != CPETGB_OK) return rc;
   ret[0] = static_cast<float>(res[0]);
   ret[1] = static_cast<float>(res[1]);
   return CPETGB_OK;
+}
+
+// The reference-shaped entry points: the same calls in the library's default precision.
+int cpetgb_compute_looped_field(int total_points, int n_charges, const float* x_0,
+                                const float* x, const float* Q, float* E) {
+  return cpetgb_compute_looped_field_p(g_default_prec.load(), total_points, n_charges, x_0, x, Q,
+                                       E);
+}
+
+int cpetgb_compute_esp_grid(int total_points, int n_charges, const float* x_0, const float* x,
+                            const float* Q, float* ESP) {
+  return cpetgb_compute_esp_grid_p(g_default_prec.load(), total_points, n_charges, x_0, x, Q,
+                                   ESP);
+}
+
+int cpetgb_calc_esp_base(float* ESP, const float* x_init, int n_charges, const float* x,
+                         const float* Q) {
+  return cpetgb_calc_esp_base_p(g_default_prec.load(), ESP, x_init, n_charges, x, Q);
+}
+
+int cpetgb_calc_field(float* E, const float* x_init, int n_charges, const float* x,
+                      const float* Q) {
+  return cpetgb_calc_field_p(g_default_prec.load(), E, x_init, n_charges, x, Q);
+}
+
+int cpetgb_thread_operation_batch(int n_lines, int n_charges, const int32_t* n_iter,
+                                  float step_size, const float* x_0, const float* dimensions,
+                                  const float* x, const float* Q, float* ret) {
+  return cpetgb_thread_operation_batch_p(g_default_prec.load(), n_lines, n_charges, n_iter,
+                                         step_size, x_0, dimensions, x, Q, ret);
+}
+
+int cpetgb_thread_operation(int n_charges, int n_iter, float step_size, const float* x_0,
+                            const float* dimensions, const float* x, const float* Q,
+                            float* ret) {
+  return cpetgb_thread_operation_p(g_default_prec.load(), n_charges, n_iter, step_size, x_0,
+                                   dimensions, x, Q, ret);
+}
+
+int cpetgb_thread_operation_dipole(int n_dipoles, int n_iter, float step_size, const float* x_0,
+                                   const float* dimensions, const float* x, const float* mu,
+                                   float* ret) {
+  return cpetgb_thread_operation_dipole_p(g_default_prec.load(), n_dipoles, n_iter, step_size,
+                                          x_0, dimensions, x, mu, ret);
 }
 
 }  // extern "C"

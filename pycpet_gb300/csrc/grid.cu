@@ -20,6 +20,18 @@
 //   FP64   every operation in IEEE double (plain sums), the drop-in form.
 // A frame whose charges are split over several items writes per-split partial
 // sums (doubles) that grid_final_kernel adds in split order: deterministic.
+//
+// The r^2 >= 1e-6 clamp of compute_looped_field only changes a pair term when
+// a point lies within 1e-3 A of a charge.  A CTA takes the bounding box of its
+// points once, tests each staged tile of charges against it (distance below
+// kNearA) and runs the clamped loop only for tiles that hold such a charge;
+// every other tile runs the unclamped loop, which gives the same values there.
+//
+// FP32C field refinement: where the field nearly cancels, FP32 rounding of the
+// pair terms (about 1e-7 of each term) is a large fraction of |E|.  After the
+// FP32C pass, grid_flag_kernel finds, per frame, the points whose |E| is below
+// tau times the frame's median |E| and grid_refine_kernel recomputes those
+// points in IEEE double over all of the frame's charges.
 #include <algorithm>
 #include <type_traits>
 
@@ -76,7 +88,64 @@ __device__ __forceinline__ void kahan_add2(uint64_t& s, uint64_t& c, uint64_t t)
 
 constexpr int kKahanRun = 32;  // FP32C: charges summed plainly between Kahan steps
 
+// A staged charge closer than kNearA to the CTA's point box sends its tile
+// through the clamped loop.  The clamp acts below 1e-3 A; the margin covers the
+// FP32 rounding of coordinates up to 1e4 A.
+constexpr float kNearA = 0.01f;
+
+__device__ __forceinline__ void charge_xyz(const ChargeDup& c, float& x, float& y, float& z) {
+  x = __uint_as_float(static_cast<uint32_t>(c.xy.x));
+  y = __uint_as_float(static_cast<uint32_t>(c.xy.y));
+  z = __uint_as_float(static_cast<uint32_t>(c.zq.x));
+}
+__device__ __forceinline__ void charge_xyz(const Charge64& c, float& x, float& y, float& z) {
+  x = static_cast<float>(c.x);
+  y = static_cast<float>(c.y);
+  z = static_cast<float>(c.z);
+}
+// Squared distance from (x, y, z) to the box [lo, hi] (0 inside).
+__device__ __forceinline__ float box_dist2(const float (&lo)[3], const float (&hi)[3], float x,
+                                           float y, float z) {
+  const float dx = fmaxf(fmaxf(lo[0] - x, x - hi[0]), 0.f);
+  const float dy = fmaxf(fmaxf(lo[1] - y, y - hi[1]), 0.f);
+  const float dz = fmaxf(fmaxf(lo[2] - z, z - hi[2]), 0.f);
+  return dx * dx + dy * dy + dz * dz;
+}
+
+// One charge against this thread's G packed point pairs, added to part[].
+template <int KIND, bool CLAMP, int G>
+__device__ __forceinline__ void pair_terms_f32x2(const ChargeDup& ch, const uint64_t (&px)[G],
+                                                 const uint64_t (&py)[G], const uint64_t (&pz)[G],
+                                                 uint64_t (&part)[(KIND == kField) ? 3 : 1][G]) {
+  const ulonglong2 xy = ch.xy;
+  const ulonglong2 zq = ch.zq;
+#pragma unroll
+  for (int g = 0; g < G; ++g) {
+    const uint64_t dx = sub2(px[g], xy.x);
+    const uint64_t dy = sub2(py[g], xy.y);
+    const uint64_t dz = sub2(pz[g], zq.x);
+    uint64_t r2 = fma2(dx, dx, fma2(dy, dy, mul2(dz, dz)));
+    if constexpr (CLAMP) {  // compute_looped_field's fmaxf(r^2, 1e-6f)
+      float a, b;
+      upk2(r2, a, b);
+      r2 = pk2(fmaxf(a, 1e-6f), fmaxf(b, 1e-6f));
+    }
+    const uint64_t ri = rsqrt2(r2);
+    if constexpr (KIND == kField) {
+      const uint64_t w = mul2(mul2(zq.y, ri), mul2(ri, ri));
+      part[0][g] = fma2(w, dx, part[0][g]);
+      part[1][g] = fma2(w, dy, part[1][g]);
+      part[2][g] = fma2(w, dz, part[2][g]);
+    } else {
+      part[0][g] = fma2(zq.y, ri, part[0][g]);
+    }
+  }
+}
+
 // FP32C body: this thread's points as G packed pairs (points k = 2g, 2g+1).
+// CLAMP = true is the rare path (a staged charge next to the point box): the
+// same arithmetic with the clamp, in a loop that is not unrolled, so it adds
+// few registers to the kernel.
 template <int KIND, bool CLAMP, int G>
 __device__ __forceinline__ void grid_tile_f32x2(const ChargeDup* __restrict__ tl, int cnt,
                                                 const uint64_t (&px)[G], const uint64_t (&py)[G],
@@ -90,31 +159,12 @@ __device__ __forceinline__ void grid_tile_f32x2(const ChargeDup* __restrict__ tl
     for (int c = 0; c < NC; ++c)
 #pragma unroll
       for (int g = 0; g < G; ++g) part[c][g] = 0ull;
+    if constexpr (CLAMP) {
+#pragma unroll 1
+      for (int j = j0; j < j1; ++j) pair_terms_f32x2<KIND, true, G>(tl[j], px, py, pz, part);
+    } else {
 #pragma unroll 4
-    for (int j = j0; j < j1; ++j) {
-      const ulonglong2 xy = tl[j].xy;
-      const ulonglong2 zq = tl[j].zq;
-#pragma unroll
-      for (int g = 0; g < G; ++g) {
-        const uint64_t dx = sub2(px[g], xy.x);
-        const uint64_t dy = sub2(py[g], xy.y);
-        const uint64_t dz = sub2(pz[g], zq.x);
-        uint64_t r2 = fma2(dx, dx, fma2(dy, dy, mul2(dz, dz)));
-        if constexpr (CLAMP) {  // compute_looped_field's fmaxf(r^2, 1e-6f)
-          float a, b;
-          upk2(r2, a, b);
-          r2 = pk2(fmaxf(a, 1e-6f), fmaxf(b, 1e-6f));
-        }
-        const uint64_t ri = rsqrt2(r2);
-        if constexpr (KIND == kField) {
-          const uint64_t w = mul2(mul2(zq.y, ri), mul2(ri, ri));
-          part[0][g] = fma2(w, dx, part[0][g]);
-          part[1][g] = fma2(w, dy, part[1][g]);
-          part[2][g] = fma2(w, dz, part[2][g]);
-        } else {
-          part[0][g] = fma2(zq.y, ri, part[0][g]);
-        }
-      }
+      for (int j = j0; j < j1; ++j) pair_terms_f32x2<KIND, false, G>(tl[j], px, py, pz, part);
     }
 #pragma unroll
     for (int c = 0; c < NC; ++c)
@@ -123,8 +173,10 @@ __device__ __forceinline__ void grid_tile_f32x2(const ChargeDup* __restrict__ tl
   }
 }
 
+// FP32C with 4 points per thread: at most 80 registers, so six CTAs (24
+// warps) share an SM.
 template <int PREC, int KIND, bool CLAMP, int PPT>
-__global__ void __launch_bounds__(kGridThreads)
+__global__ void __launch_bounds__(kGridThreads, PREC == kFP32C && PPT == 4 ? 6 : 0)
     grid_kernel(const GridItem* __restrict__ items, const void* __restrict__ packed,
                 const double* __restrict__ points, double* __restrict__ out,
                 double* __restrict__ partial, int* __restrict__ status) {
@@ -194,18 +246,81 @@ __global__ void __launch_bounds__(kGridThreads)
 #pragma unroll
     for (int k = 0; k < PPT; ++k) acc[c][k] = Real(0);
 
+  // Bounding box of this CTA's points (clamped kernels only), kept in shared
+  // memory so it holds no registers during the pair loops.
+  __shared__ float box_s[6];
+  if constexpr (CLAMP) {
+    __shared__ float box_part[kGridThreads / 32][6];
+    float v[6] = {3.0e38f, 3.0e38f, 3.0e38f, -3.0e38f, -3.0e38f, -3.0e38f};
+#pragma unroll
+    for (int k = 0; k < PPT; ++k) {
+      if (tid + k * kGridThreads < it.p_count) {
+        const float c3[3] = {static_cast<float>(px[k]), static_cast<float>(py[k]),
+                             static_cast<float>(pz[k])};
+#pragma unroll
+        for (int a = 0; a < 3; ++a) {
+          v[a] = fminf(v[a], c3[a]);
+          v[3 + a] = fmaxf(v[3 + a], c3[a]);
+        }
+      }
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1)
+#pragma unroll
+      for (int a = 0; a < 3; ++a) {
+        v[a] = fminf(v[a], __shfl_xor_sync(0xffffffffu, v[a], o));
+        v[3 + a] = fmaxf(v[3 + a], __shfl_xor_sync(0xffffffffu, v[3 + a], o));
+      }
+    if ((tid & 31) == 0)
+#pragma unroll
+      for (int a = 0; a < 6; ++a) box_part[tid >> 5][a] = v[a];
+    __syncthreads();
+    if (tid < 6) {
+      float b = box_part[0][tid];
+#pragma unroll
+      for (int w = 1; w < kGridThreads / 32; ++w)
+        b = tid < 3 ? fminf(b, box_part[w][tid]) : fmaxf(b, box_part[w][tid]);
+      box_s[tid] = b;
+    }
+    __syncthreads();
+  }
+
   bool ok = true;
   for (int t = 0; t < n_tiles; ++t) {
     const int s = t % kStages;
     const bool mine = mbar_wait(&full[s], static_cast<uint32_t>((t / kStages) & 1), status);
-    ok = __syncthreads_and(mine) != 0;  // also: every thread is done with tile t-1
+    const int cnt = min(TC, n - t * TC);
+    const ChargeT* tl = &tile[s][0];
+    bool clamp_tile = false;
+    if constexpr (CLAMP) {
+      // Does this tile hold a charge next to the point box?  One barrier both
+      // answers that and confirms every thread's wait (the common case).
+      bool near = false;
+      if (mine) {
+        const float blo[3] = {box_s[0], box_s[1], box_s[2]};
+        const float bhi[3] = {box_s[3], box_s[4], box_s[5]};
+        for (int j = tid; j < cnt; j += kGridThreads) {
+          float cx, cy, cz;
+          charge_xyz(tl[j], cx, cy, cz);
+          near |= box_dist2(blo, bhi, cx, cy, cz) < kNearA * kNearA;
+        }
+      }
+      const int clean = __syncthreads_count(mine && !near);  // also: tile t-1 is done
+      if (clean != kGridThreads) {
+        ok = __syncthreads_and(mine) != 0;
+        clamp_tile = true;
+      }
+    } else {
+      ok = __syncthreads_and(mine) != 0;  // also: every thread is done with tile t-1
+    }
     if (!ok) break;
     if (tid == 0 && t >= 1 && (t - 1) + kStages < n_tiles) issue((t - 1) + kStages);
 
-    const int cnt = min(TC, n - t * TC);
-    const ChargeT* tl = &tile[s][0];
     if constexpr (PREC == kFP32C) {
-      grid_tile_f32x2<KIND, CLAMP, G>(tl, cnt, px2, py2, pz2, acc2, cmp2);
+      if (CLAMP && clamp_tile)
+        grid_tile_f32x2<KIND, true, G>(tl, cnt, px2, py2, pz2, acc2, cmp2);
+      else
+        grid_tile_f32x2<KIND, false, G>(tl, cnt, px2, py2, pz2, acc2, cmp2);
     } else {
       Real part[NC][PPT];
 #pragma unroll
@@ -221,7 +336,7 @@ __global__ void __launch_bounds__(kGridThreads)
           const Real dy = py[k] - ch.y;
           const Real dz = pz[k] - ch.z;
           Real r2 = dx * dx + dy * dy + dz * dz;
-          if constexpr (CLAMP) r2 = fmax(r2, Real(1e-6));  // compute_looped_field's fmaxf
+          if (CLAMP && clamp_tile) r2 = fmax(r2, Real(1e-6));  // compute_looped_field's fmaxf
           const Real ri = rsqrt_f64(r2);
           if constexpr (KIND == kField) {
             const Real w = (charge_q(ch) * ri) * (ri * ri);
@@ -277,6 +392,127 @@ __global__ void grid_final_kernel(const GridFinal* __restrict__ fin,
     for (int s = 0; s < f.n_split; ++s)
       v += partial[(static_cast<int64_t>(f.slot_base + s) * kGridSlotPts + pl) * 3 + c];
     out[NC * (f.out_row + pl) + c] = v;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// FP32C field refinement (see the header comment).
+// ---------------------------------------------------------------------------
+constexpr int kFlagThreads = 512;
+constexpr int kMagBins = 4096;  // bits 30..19 of the float |E|: exponent + 4 mantissa bits
+constexpr int kBinsPerThread = kMagBins / kFlagThreads;
+constexpr int kRefineThreads = 256;
+
+__device__ __forceinline__ double field_norm(const double* e) {
+  return sqrt(e[0] * e[0] + e[1] * e[1] + e[2] * e[2]);
+}
+
+// One CTA per frame (desc rows {charge_off, n, point_off, P}).  Histograms the
+// frame's |E| in 1/16-octave bins, takes the lower edge of the bin holding the
+// lower median as the frame's scale, and appends every point with |E| below
+// tau times that scale to list[] as {output row, frame}.  The counts are exact
+// integers, so the threshold -- and the set of points -- is deterministic.
+__global__ void __launch_bounds__(kFlagThreads)
+    grid_flag_kernel(const int64_t* __restrict__ desc, const double* __restrict__ out, double tau,
+                     int64_t* __restrict__ list, int* __restrict__ count) {
+  __shared__ int hist[kMagBins];
+  __shared__ int part[kFlagThreads];
+  __shared__ float scale_s;
+  const int64_t po = desc[4 * blockIdx.x + 2], P = desc[4 * blockIdx.x + 3];
+  for (int b = threadIdx.x; b < kMagBins; b += kFlagThreads) hist[b] = 0;
+  __syncthreads();
+  for (int64_t i = threadIdx.x; i < P; i += kFlagThreads) {
+    const double m = field_norm(out + 3 * (po + i));
+    if (m <= 3.0e38)  // finite in float (NaN compares false)
+      atomicAdd(&hist[__float_as_uint(static_cast<float>(m)) >> 19], 1);
+  }
+  __syncthreads();
+  int own = 0;
+#pragma unroll
+  for (int k = 0; k < kBinsPerThread; ++k) own += hist[threadIdx.x * kBinsPerThread + k];
+  part[threadIdx.x] = own;
+  __syncthreads();
+  if (threadIdx.x < 32) {
+    constexpr int kPerLane = kFlagThreads / 32;
+    const int lane = threadIdx.x;
+    int mine = 0;
+#pragma unroll
+    for (int k = 0; k < kPerLane; ++k) mine += part[lane * kPerLane + k];
+    int incl = mine;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const int v = __shfl_up_sync(0xffffffffu, incl, o);
+      if (lane >= o) incl += v;
+    }
+    const int total = __shfl_sync(0xffffffffu, incl, 31);
+    if (total == 0) {
+      if (lane == 0) scale_s = 0.f;  // no finite value: nothing to refine
+    } else {
+      const int rank = (total - 1) / 2;
+      const unsigned passed = __ballot_sync(0xffffffffu, incl > rank);
+      if (lane == __ffs(passed) - 1) {
+        int cum = incl - mine, t = lane * kPerLane;
+        while (cum + part[t] <= rank) cum += part[t++];
+        int b = t * kBinsPerThread;
+        while (cum + hist[b] <= rank) cum += hist[b++];
+        scale_s = __uint_as_float(static_cast<uint32_t>(b) << 19);
+      }
+    }
+  }
+  __syncthreads();
+  const double thr = tau * static_cast<double>(scale_s);
+  for (int64_t i = threadIdx.x; i < P; i += kFlagThreads) {
+    if (field_norm(out + 3 * (po + i)) < thr) {
+      const int k = atomicAdd(count, 1);
+      list[2 * k] = po + i;
+      list[2 * k + 1] = blockIdx.x;
+    }
+  }
+}
+
+// Recomputes the listed points in IEEE double: one CTA per point at a time,
+// the frame's charges split over the threads, combined by a fixed tree.
+template <bool CLAMP>
+__global__ void __launch_bounds__(kRefineThreads)
+    grid_refine_kernel(const int64_t* __restrict__ desc, const int64_t* __restrict__ list,
+                       const int* __restrict__ count, const double* __restrict__ points,
+                       const double* __restrict__ x, const double* __restrict__ q,
+                       double* __restrict__ out) {
+  __shared__ double red[kRefineThreads / 32][3];
+  const int n_list = *count;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  for (int e = blockIdx.x; e < n_list; e += gridDim.x) {
+    const int64_t row = list[2 * e];
+    const int64_t f = list[2 * e + 1];
+    const int64_t co = desc[4 * f], n = desc[4 * f + 1];
+    const double px = points[3 * row], py = points[3 * row + 1], pz = points[3 * row + 2];
+    double s[3] = {0.0, 0.0, 0.0};
+    for (int64_t j = threadIdx.x; j < n; j += kRefineThreads) {
+      const double* c = x + 3 * (co + j);
+      const double dx = px - c[0], dy = py - c[1], dz = pz - c[2];
+      double r2 = dx * dx + dy * dy + dz * dz;
+      if (CLAMP) r2 = fmax(r2, 1e-6);  // compute_looped_field's clamp
+      const double ri = rsqrt(r2);
+      const double w = (q[co + j] * ri) * (ri * ri);
+      s[0] += w * dx;
+      s[1] += w * dy;
+      s[2] += w * dz;
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1)
+#pragma unroll
+      for (int a = 0; a < 3; ++a) s[a] += __shfl_xor_sync(0xffffffffu, s[a], o);
+    if (lane == 0)
+#pragma unroll
+      for (int a = 0; a < 3; ++a) red[warp][a] = s[a];
+    __syncthreads();
+    if (threadIdx.x < 3) {
+      double v = 0.0;
+#pragma unroll
+      for (int w = 0; w < kRefineThreads / 32; ++w) v += red[w][threadIdx.x];
+      out[3 * row + threadIdx.x] = v * kCoulomb;
+    }
+    __syncthreads();
   }
 }
 
@@ -402,6 +638,29 @@ cudaError_t preload_grid_kernels(int prec, int kind, int clamp, int ppt) {
   if (e != cudaSuccess) return e;
   return prec == kFP32C ? cudaFuncGetAttributes(&a, pack_dup_f32_kernel)
                         : cudaFuncGetAttributes(&a, pack_f64_kernel);
+}
+
+cudaError_t launch_grid_refine(int n_frames, const int64_t* desc, const double* points,
+                               const double* x, const double* q, double* out, int clamp,
+                               double tau, int64_t* list, int* count, int num_sms, cudaStream_t s) {
+  if (n_frames <= 0 || !(tau > 0.0)) return cudaSuccess;
+  cudaError_t e = cudaMemsetAsync(count, 0, sizeof(int), s);
+  if (e != cudaSuccess) return e;
+  grid_flag_kernel<<<n_frames, kFlagThreads, 0, s>>>(desc, out, tau, list, count);
+  const int ctas = std::max(num_sms, 1) * 8;
+  if (clamp)
+    grid_refine_kernel<true><<<ctas, kRefineThreads, 0, s>>>(desc, list, count, points, x, q, out);
+  else
+    grid_refine_kernel<false><<<ctas, kRefineThreads, 0, s>>>(desc, list, count, points, x, q, out);
+  return cudaGetLastError();
+}
+
+cudaError_t preload_grid_refine() {
+  cudaFuncAttributes a;
+  cudaError_t e = cudaFuncGetAttributes(&a, grid_flag_kernel);
+  if (e == cudaSuccess) e = cudaFuncGetAttributes(&a, grid_refine_kernel<true>);
+  if (e == cudaSuccess) e = cudaFuncGetAttributes(&a, grid_refine_kernel<false>);
+  return e;
 }
 
 cudaError_t launch_grid_final(int kind, int n_final, const GridFinal* fin, const double* partial,

@@ -93,3 +93,34 @@ def make_dipole_frame(n_dipoles: int, seed: int, sigma: float = 0.3):
     fr = make_frame(n_dipoles, seed)
     mu = np.random.default_rng(seed + 104729).normal(0.0, sigma, (n_dipoles, 3))
     return {"x": fr["x"], "mu": mu, "seed": seed}
+
+
+def volume_batch_specs(n_frames: int, seed: int = 2024):
+    """Frame shapes of the batched volume workload: per frame (n_charges,
+    half_width, frame_seed) with N ~ U[3,000, 40,000] and half-widths 0.5, 1.0
+    or 1.5 A (11^3, 21^3 or 31^3 points at 0.1 A)."""
+    rng = np.random.default_rng(seed)
+    specs = []
+    for f in range(n_frames):
+        n = int(rng.integers(3000, 40001))
+        half = float(rng.choice([0.5, 1.0, 1.5]))
+        specs.append((n, half, 5000 + f))
+    return specs
+
+
+def cube_points(half: float, step: float = 0.1):
+    """The (2*half/step + 1)^3 grid points of a cube centred at the origin, ij order."""
+    g = np.linspace(-half, half, int(round(2 * half / step)) + 1)
+    return np.stack(np.meshgrid(g, g, g, indexing="ij"), -1).reshape(-1, 3)
+
+
+def volume_batch_frames(n_frames: int, seed: int = 2024, only=None):
+    """[(points, x, q)] of the batched volume workload (volume_batch_specs);
+    ``only`` restricts it to the listed frame indices."""
+    out = []
+    for f, (n, half, fs) in enumerate(volume_batch_specs(n_frames, seed)):
+        if only is not None and f not in only:
+            continue
+        fr = make_frame(n, seed=fs)
+        out.append((cube_points(half), fr["x"], fr["q"]))
+    return out
