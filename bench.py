@@ -55,12 +55,9 @@ def workload_config(precision="fp32c"):
 
 
 def make_inputs(rank: int):
-    from pycpet_gb300.synth import make_frame, random_start_points
+    from pycpet_gb300.synth import topo_workload
 
-    fr = make_frame(N_CHARGES, seed=1 + 1000 * rank)
-    starts = random_start_points(N_LINES, [HALF] * 3, seed=2 + 1000 * rank)
-    caps = np.full(N_LINES, CAP, dtype=np.int32)
-    return fr["x"], fr["q"], starts, caps
+    return topo_workload(rank)
 
 
 def pair_evals(steps, n_charges):

@@ -75,6 +75,14 @@ int cpetgb_get_default_precision(void);
 int cpetgb_set_field_refinement(double tau);
 double cpetgb_field_refinement(void);
 
+/* Failure-path check of the device-side waits: runs one CTA whose bounded
+ * mbarrier wait can never be satisfied (no copy is issued), with a limit of
+ * `seconds` (0 < seconds <= 2) instead of the kernels' 2 s.  The wait runs out,
+ * the kernel records the timeout in the device status word and returns, and
+ * this call reports it like any other call: CPETGB_ETIMEOUT means the bounded
+ * wait works (the device stays usable).  No counterpart in the reference,
+ * whose CPU code has no device waits. */
+int cpetgb_check_wait_limit(double seconds);
 /* Pipe throughput microbenchmark on the current device (roofline denominators):
  * kind 0 FP32 FFMA flop/s, 1 FP64 DFMA flop/s, 2 MUFU rsqrt op/s, 3 FP32x2 FFMA2 flop/s,
  * 4 pair evaluations/s of the FP32C streamline sweep's inner loop alone. */

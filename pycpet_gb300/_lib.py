@@ -53,6 +53,7 @@ SIGNATURES = {
     "cpetgb_thread_operation_dipole_p": [_i, _i, _i, _f, _vp, _vp, _vp, _vp, _vp],
     "cpetgb_compute_esp_grid_p": [_i, _i, _i, _vp, _vp, _vp, _vp],
     "cpetgb_set_field_refinement": [_d],
+    "cpetgb_check_wait_limit": [_d],
     "cpetgb_field_grid": [_i, _i, _i, _i, _vp, _vp, _vp, _i, _vp, _vp],
     "cpetgb_esp_grid": [_i, _i, _i, _i, _vp, _vp, _vp, _vp, _vp],
     "cpetgb_grid_batch": [_i, _i, _i, _i, _i, _vp, _vp, _vp, _vp, _vp, _vp],

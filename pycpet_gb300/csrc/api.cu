@@ -1045,6 +1045,17 @@ int cpetgb_synchronize(void* stream) {
   return finish(c, static_cast<cudaStream_t>(stream));
 }
 
+int cpetgb_check_wait_limit(double seconds) {
+  if (!(seconds > 0.0) || seconds > 2.0)
+    return fail(CPETGB_EINVAL, "wait limit must be in (0, 2] s, got %g", seconds);
+  int rc;
+  Ctx* c = context(&rc);
+  if (!c) return rc;
+  const unsigned long long ns = static_cast<unsigned long long>(seconds * 1e9);
+  CK(launch_wait_limit_check(c->status, ns, c->stream), "wait check launch");
+  return finish(c, c->stream);
+}
+
 int cpetgb_set_field_refinement(double tau) {
   if (!(tau >= 0.0) || !std::isfinite(tau) || tau > 1.0)
     return fail(CPETGB_EINVAL, "refinement threshold must be in [0, 1], got %g", tau);

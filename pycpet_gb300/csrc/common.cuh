@@ -64,14 +64,15 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
   return ok != 0;
 }
 
-// Bounded wait on phase `parity`.  On timeout records kDevWaitTimeout in
-// *status (first error wins) and returns false.
-__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, int* status) {
+// Bounded wait on phase `parity`.  On timeout (limit_ns of %globaltimer)
+// records kDevWaitTimeout in *status (first error wins) and returns false.
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, int* status,
+                                          unsigned long long limit_ns = kWaitLimitNs) {
   if (mbar_try_wait(bar, parity)) return true;
   const unsigned long long t0 = globaltimer_ns();
   for (uint32_t it = 1;; ++it) {
     if (mbar_try_wait(bar, parity)) return true;
-    if ((it & 255u) == 0 && globaltimer_ns() - t0 > kWaitLimitNs) {
+    if ((it & 255u) == 0 && globaltimer_ns() - t0 > limit_ns) {
       if (status) atomicCAS(status, kDevOk, kDevWaitTimeout);
       return false;
     }

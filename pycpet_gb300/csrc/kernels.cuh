@@ -141,6 +141,10 @@ int topo_charge_pad(int prec);         // packed charge arrays are padded to thi
 cudaError_t launch_pack_topo(int prec, int64_t n, int64_t n_pad, const double* x, const double* q,
                              void* packed, cudaStream_t s);
 
+// peaks.cu: one CTA whose bounded mbarrier wait can never be satisfied runs
+// out after limit_ns and records kDevWaitTimeout in *status.
+cudaError_t launch_wait_limit_check(int* status, unsigned long long limit_ns, cudaStream_t s);
+
 // api.cu: records `msg` as the calling thread's last error and returns `code`.
 int set_error(int code, const char* msg);
 

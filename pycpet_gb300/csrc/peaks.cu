@@ -1,4 +1,5 @@
-// peaks.cu -- throughput microbenchmarks for the roofline denominators.
+// peaks.cu -- throughput microbenchmarks for the roofline denominators, and
+// the check of the bounded device-side waits (wait_limit_kernel).
 //
 // The all-pairs Coulomb sums are bound by the FP32 pipe (FP32C form), the
 // FP64 pipe (FP64 form) or the MUFU reciprocal square root.  Each kernel
@@ -153,7 +154,27 @@ __global__ void __launch_bounds__(kSweepThreads, 1) sweep_loop_kernel(const floa
   if (s == 1234.5f) out[0] = s;
 }
 
+// A bounded wait that nothing completes: the mbarrier expects one arrival
+// that never comes and no copy is issued, so each thread's wait runs out
+// after limit_ns, records kDevWaitTimeout and returns (the path every
+// kernel's waits take when a bulk copy does not complete).
+__global__ void wait_limit_kernel(int* status, unsigned long long limit_ns) {
+  __shared__ alignas(8) uint64_t bar;
+  if (threadIdx.x == 0) {
+    mbar_init(&bar, 1);
+    fence_mbar_init();
+  }
+  __syncthreads();
+  mbar_wait(&bar, 0, status, limit_ns);
+}
+
 }  // namespace
+
+cudaError_t launch_wait_limit_check(int* status, unsigned long long limit_ns, cudaStream_t s) {
+  wait_limit_kernel<<<1, 32, 0, s>>>(status, limit_ns);
+  return cudaGetLastError();
+}
+
 }  // namespace cpetgb
 
 namespace {

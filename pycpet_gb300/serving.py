@@ -15,6 +15,15 @@ time against frames whose charges stay resident on the device.
 * Admission: a request is started only while the memory it needs fits an HBM
   budget (80% of the device by default) next to the resident frames; the
   engine also refuses (and the loop retries) when its line store is full.
+* Refusals and the watchdog: a request that can never run -- an unknown kind
+  or frame, no points or lines, non-finite coordinates, a step cap outside
+  [0, 2^24], more memory than the budget leaves beside the resident frames --
+  is refused at submit() with status "rejected" and a message, and counts as
+  completed; with ``pending_deadline_s`` set, a request still waiting for
+  admission that long after its arrival is cancelled with status "expired".
+  Frames with no charges or with non-finite positions or charges are refused
+  by add_frame().  The reference has no request loop; its only recovery is to
+  skip inputs whose output file exists (CPET/source/CPET.py:119-126).
 
 Latency is measured from a request's arrival to its results on the host.
 """
@@ -47,6 +56,8 @@ class Request:
     result: np.ndarray | None = None
     t_start: float | None = None
     t_done: float | None = None
+    status: str = "new"                   # pending, running, done, rejected, expired
+    error: str | None = None
     _rid: int = -1
 
     @property
@@ -57,6 +68,55 @@ class Request:
         if self.kind == "topo":
             return int(len(self.starts) * 48)
         return int(len(self.points) * 48)
+
+
+MAX_STEP_CAP = 1 << 24   # the library's largest per-line step cap
+
+
+def validate_request(req: Request, frames, max_bytes: int) -> str | None:
+    """Why `req` can never be served (a message), or None.  `frames` holds the
+    resident frame ids; `max_bytes` is what the budget leaves beside them."""
+    if req.kind not in KINDS:
+        return f"unknown request kind {req.kind!r}"
+    if req.frame not in frames:
+        return f"frame {req.frame} is not resident"
+    if req.kind == "topo":
+        if req.starts is None:
+            return "a topo request needs start points"
+        st = np.asarray(req.starts, np.float64).reshape(-1, 3)
+        if len(st) == 0:
+            return "a topo request needs at least one start point"
+        if not np.all(np.isfinite(st)):
+            return "start points must be finite"
+        caps = np.asarray(req.n_iter if req.n_iter is not None else 0)
+        if caps.size not in (1, len(st)) or np.any(caps < 0) or np.any(caps > MAX_STEP_CAP):
+            return f"step caps must be one value or one per line, in [0, {MAX_STEP_CAP}]"
+        if not np.isfinite(req.step):
+            return "the step must be finite"
+        half = np.asarray(req.half_dims, np.float64)
+        if half.size != 3 or not np.all(np.isfinite(half)) or np.any(half < 0):
+            return "half_dims must be three finite values >= 0"
+    else:
+        if req.points is None:
+            return "a grid or point request needs points"
+        pts = np.asarray(req.points, np.float64).reshape(-1, 3)
+        if len(pts) == 0:
+            return "a grid or point request needs at least one point"
+        if not np.all(np.isfinite(pts)):
+            return "points must be finite"
+    if req.bytes_needed() > max_bytes:
+        return f"needs {req.bytes_needed()} bytes, more than the {max_bytes} the HBM budget leaves"
+    return None
+
+
+def expire_pending(pending, now: float, deadline_s: float | None):
+    """Splits waiting requests into (kept, expired) by the pending deadline."""
+    if deadline_s is None:
+        return list(pending), []
+    kept, expired = [], []
+    for r in pending:
+        (expired if now - r.arrival > deadline_s else kept).append(r)
+    return kept, expired
 
 
 @dataclass
@@ -72,11 +132,13 @@ class _GridLaunch:
 class Server:
     def __init__(self, precision="fp32c", hbm_budget_frac=0.8, line_capacity=2_000_000,
                  charge_capacity=4_000_000, max_frames=64, max_requests=4096, chunk_lines=32,
-                 engine_ctas_per_sm=1):
+                 engine_ctas_per_sm=1, pending_deadline_s=None):
         """``engine_ctas_per_sm``: 1 keeps half of every SM free for grid and
         point requests (mixed serving); 2 gives the streamline engine whole SMs
         (streamline-only serving: about 1.5x the line throughput, but a grid
-        request then waits until the engine's launch ends)."""
+        request then waits until the engine's launch ends).
+        ``pending_deadline_s``: cancel requests not admitted that long after
+        their arrival (None: wait indefinitely)."""
         import torch
 
         self.torch = torch
@@ -102,11 +164,16 @@ class Server:
         self.topo_running: list[Request] = []
         self.completed: list[Request] = []
         self.max_topo_inflight = 0
+        self.pending_deadline_s = pending_deadline_s
 
     # ---- frames ---------------------------------------------------------------
     def add_frame(self, frame_id, x, q):
         x = np.ascontiguousarray(np.asarray(x, np.float64).reshape(-1, 3))
         q = np.ascontiguousarray(np.asarray(q, np.float64).reshape(-1))
+        if len(q) == 0 or len(x) != len(q):
+            raise ValueError(f"frame {frame_id}: needs one position per charge and at least one charge")
+        if not (np.all(np.isfinite(x)) and np.all(np.isfinite(q))):
+            raise ValueError(f"frame {frame_id}: positions and charges must be finite")
         fid = ctypes.c_int(-1)
         check(lib().cpetgb_engine_add_frame(self.engine, len(q), x.ctypes.data, q.ctypes.data, ctypes.byref(fid)))
         off = sum(len(a) for a in self._gq)
@@ -124,12 +191,18 @@ class Server:
         return self._pool_x, self._pool_q
 
     # ---- requests ---------------------------------------------------------------
-    def submit(self, req: Request):
-        if req.kind not in KINDS:
-            raise ValueError(f"unknown request kind {req.kind!r}")
-        if req.frame not in self.frames:
-            raise KeyError(f"frame {req.frame} is not resident")
+    def submit(self, req: Request) -> bool:
+        """Queues `req` (True) or refuses it at once (False: status
+        "rejected", the reason in ``req.error``, counted as completed)."""
+        why = validate_request(req, self.frames, self.budget - self.resident_bytes)
+        if why is not None:
+            req.status, req.error = "rejected", why
+            req.t_done = time.perf_counter()
+            self.completed.append(req)
+            return False
+        req.status = "pending"
         self.pending.append(req)
+        return True
 
     def _fits(self, nbytes):
         return self.resident_bytes + self.inflight_bytes + nbytes <= self.budget
@@ -147,6 +220,7 @@ class Server:
         check(rc)
         req._rid = rid.value
         req.t_start = now
+        req.status = "running"
         self.topo_running.append(req)
         self.max_topo_inflight = max(self.max_topo_inflight, len(self.topo_running))
         return True
@@ -162,6 +236,7 @@ class Server:
             pts.append(p)
             po += len(p)
             r.t_start = now
+            r.status = "running"
         desc = np.ascontiguousarray(np.array(desc, dtype=np.int64))
         host_pts = t.from_numpy(np.concatenate(pts)).pin_memory()
         nc = 3 if kind_code == FIELD else 1
@@ -185,6 +260,12 @@ class Server:
         """One pass of the loop: admit, launch, poll.  Returns True if anything moved."""
         now = time.perf_counter() if now is None else now
         moved = False
+        self.pending, expired = expire_pending(self.pending, now, self.pending_deadline_s)
+        for r in expired:
+            r.status, r.error = "expired", f"not admitted within {self.pending_deadline_s} s"
+            r.t_done = now
+            self.completed.append(r)
+            moved = True
         # streamlines: into the engine while it accepts them
         still = []
         for r in self.pending:
@@ -226,6 +307,7 @@ class Server:
                     r.result = out[po:po + n].copy() if g.nc == 3 else out[po:po + n, 0].copy()
                     po += n
                     r.t_done = done_now
+                    r.status = "done"
                     self.completed.append(r)
                 self.inflight_bytes -= g.nbytes
                 moved = True
@@ -243,6 +325,7 @@ class Server:
                 check(lib().cpetgb_engine_collect(self.engine, r._rid, res.ctypes.data, None))
                 r.result = res
                 r.t_done = time.perf_counter()
+                r.status = "done"
                 self.completed.append(r)
                 moved = True
             else:
@@ -290,7 +373,8 @@ def latency_stats(reqs):
     """p50 / p99 latency (ms) per kind and overall."""
     out = {}
     for kind in KINDS + ("all",):
-        lat = [r.latency for r in reqs if r.latency is not None and (kind == "all" or r.kind == kind)]
+        lat = [r.latency for r in reqs
+               if r.latency is not None and r.status == "done" and (kind == "all" or r.kind == kind)]
         if lat:
             out[kind] = {"n": len(lat), "p50_ms": 1e3 * float(np.percentile(lat, 50)),
                          "p99_ms": 1e3 * float(np.percentile(lat, 99))}

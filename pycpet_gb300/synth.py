@@ -124,3 +124,18 @@ def volume_batch_frames(n_frames: int, seed: int = 2024, only=None):
         fr = make_frame(n, seed=fs)
         out.append((cube_points(half), fr["x"], fr["q"]))
     return out
+
+
+# The streamline workload the headline benchmark is quoted on: one frame of
+# 8,000 charges, 100,000 seeded uniform start points in a box of half-width
+# 1.5 A, at most 6,000 Euler steps of 0.001 A per line.
+TOPO_N_CHARGES, TOPO_N_LINES, TOPO_HALF, TOPO_STEP, TOPO_CAP = 8000, 100_000, 1.5, 0.001, 6000
+
+
+def topo_workload(rank: int = 0):
+    """(x, q, starts, caps) of the headline streamline workload; rank r > 0
+    gets its own frame and start points (seeds offset by 1000 r)."""
+    fr = make_frame(TOPO_N_CHARGES, seed=1 + 1000 * rank)
+    starts = random_start_points(TOPO_N_LINES, [TOPO_HALF] * 3, seed=2 + 1000 * rank)
+    caps = np.full(TOPO_N_LINES, TOPO_CAP, dtype=np.int32)
+    return fr["x"], fr["q"], starts, caps

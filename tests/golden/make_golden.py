@@ -1,6 +1,7 @@
 """Generates the golden fixtures of tests/golden from the reference itself.
 
-Needs a checkout of pujanajmera/pycpet (``--ref``, default /root/reference) and
+Needs a checkout of pujanajmera/pycpet (``--ref``, default: the CPETGB_REF
+environment variable, else /root/reference) and
 its C library compiled from source by ``make -C oracle`` (into
 oracle/_ref/math_module.so; the prebuilt binaries shipped in the checkout are
 never loaded).  Third-party modules the reference imports but this path does
@@ -35,6 +36,13 @@ Fixtures written (all small, compressed .npz):
                             construct_distance_matrix, and eight synthetic
                             vector fields (343 points) through its
                             construct_distance_matrix_volume
+  ref_dispatch.npz          one frame of example 1A through the reference's
+                            own dispatcher, CPET(options).run(), for
+                            point_field, volume, volume_ESP and topo: the
+                            calculator state each method reads (charges after
+                            parsing, filtering and rotation; mesh; start
+                            points and caps) and the bytes of every output
+                            file the dispatcher wrote
 """
 from __future__ import annotations
 
@@ -51,6 +59,7 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 REPO = os.path.dirname(os.path.dirname(HERE))
 REF_SO = os.path.join(REPO, "oracle", "_ref", "math_module.so")
+REF_ROOT = os.environ.get("CPETGB_REF", "/root/reference")
 
 
 def _stub_modules():
@@ -92,6 +101,7 @@ def import_reference(ref_root):
     sys.path.insert(0, ref_root)
     import CPET.utils.calculator as ucalc
     import CPET.source.calculator as scalc
+    import CPET.source.CPET  # noqa: F401  (the dispatcher, for ref_dispatch)
 
     return ucalc, scalc
 
@@ -269,9 +279,76 @@ def ref_cluster(ucalc, out):
                         dmat=dmat, fields=np.stack(fields), vmat=vmat)
 
 
+DISPATCH_OPTIONS = {
+    "inputfiletype": "pdb",
+    "center": {"method": "mean", "atoms": [{"C7": 378}, {"O9": 378}]},
+    "x": {"method": "first", "atoms": [{"O9": 378}]},
+    "y": {"method": "first", "atoms": [{"N8": 378}]},
+    "filter_intersect": True,
+    "filter": {"resid": ["CF1"], "resnum": [378]},
+    "filter_radius": 40,
+    "dimensions": [0.5, 0.5, 0.5],
+    "step_size": 0.1,
+    "n_samples": 64,
+    "max_streamline_init": "fixed_rand",
+    "concur_slip": 2,
+}
+DISPATCH_METHODS = ("point_field", "volume", "volume_ESP", "topo")
+DISPATCH_PDB = os.path.join("examples", "1A_point-field", "pdb", "1_alcdehydro_run1.pdb")
+
+
+def dispatch_options(method, inputpath, outputpath):
+    """Options of one dispatcher run (the example 3A box on example 1A's first frame)."""
+    return dict(DISPATCH_OPTIONS, CPET_method=method, inputpath=inputpath, outputpath=outputpath)
+
+
+def run_dispatcher(method, pdb, workdir):
+    """CPET(options).run() of the imported reference on a directory holding
+    `pdb`; returns {output file name: bytes}."""
+    import shutil
+
+    from CPET.source.CPET import CPET
+
+    inp, outp = os.path.join(workdir, "in"), os.path.join(workdir, "out")
+    os.makedirs(inp, exist_ok=True)
+    shutil.copy(pdb, inp)
+    CPET(dispatch_options(method, inp, outp)).run()
+    files = {}
+    for f in sorted(os.listdir(outp)):
+        with open(os.path.join(outp, f), "rb") as fh:
+            files[f] = fh.read()
+    return files
+
+
+def ref_dispatch(ref_root, scalc, out):
+    import tempfile
+
+    pdb = os.path.join(ref_root, DISPATCH_PDB)
+    rec = {}
+    for m in DISPATCH_METHODS:
+        calc = scalc.calculator(dispatch_options(m, "", ""), path_to_pdb=pdb)
+        rec[f"{m}/x"] = np.asarray(calc.x)
+        rec[f"{m}/Q"] = np.asarray(calc.Q).reshape(-1)
+        rec[f"{m}/center"] = np.asarray(calc.center)
+        rec[f"{m}/transformation_matrix"] = np.asarray(calc.transformation_matrix)
+        if m in ("volume", "volume_ESP"):
+            rec[f"{m}/mesh"] = np.asarray(calc.mesh)
+            rec[f"{m}/dimensions"] = np.asarray(calc.dimensions)
+            rec[f"{m}/step_size"] = np.float64(calc.step_size)
+        if m == "topo":
+            rec[f"{m}/starts"] = np.asarray(calc.random_start_points)
+            rec[f"{m}/caps"] = np.asarray(calc.random_max_samples).reshape(-1)
+            rec[f"{m}/dimensions"] = np.asarray(calc.dimensions)
+            rec[f"{m}/step_size"] = np.float64(calc.step_size)
+        with tempfile.TemporaryDirectory() as tmp:
+            for name, data in run_dispatcher(m, pdb, tmp).items():
+                rec[f"{m}/file/{name}"] = np.frombuffer(data, dtype=np.uint8)
+    np.savez_compressed(out, **rec)
+
+
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--ref", default="/root/reference")
+    ap.add_argument("--ref", default=REF_ROOT)
     a = ap.parse_args()
     ucalc, scalc = import_reference(a.ref)
     examples_point_field(a.ref, scalc, os.path.join(HERE, "examples_point_field.npz"))
@@ -282,6 +359,7 @@ def main():
     ref_dat(a.ref, os.path.join(HERE, "ref_dat.npz"))
     ref_prep(ucalc, os.path.join(HERE, "ref_prep.npz"))
     ref_topo_dipole(scalc, os.path.join(HERE, "ref_topo_dipole.npz"))
+    ref_dispatch(a.ref, scalc, os.path.join(HERE, "ref_dispatch.npz"))
     for f in sorted(glob.glob(os.path.join(HERE, "*.npz"))):
         print(f, os.path.getsize(f))
 

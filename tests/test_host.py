@@ -48,9 +48,9 @@ def test_grid_counts_and_mesh():
 
 
 def test_restatements_match_reference_functions():
-    ref = "/root/reference"
+    ref = os.environ.get("CPETGB_REF", "/root/reference")
     if not os.path.isdir(ref) or not os.path.exists(os.path.join(ROOT, "oracle", "_ref", "math_module.so")):
-        pytest.skip("reference checkout not present")
+        pytest.skip(f"reference checkout or its library not present (CPETGB_REF={ref})")
     import sys
     sys.path.insert(0, os.path.join(ROOT, "tests", "golden"))
     from make_golden import import_reference
