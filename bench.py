@@ -42,16 +42,29 @@ FLOPS_PER_PAIR = 17        # 3 sub, r^2 (1 mul + 2 fma), r^-3 (2 mul), q (1 mul)
 L2_FLUSH_BYTES = 256 << 20
 
 
-def workload_config(precision="fp32c"):
+def workload_config():
+    """The workload (identical in both arms; the arithmetic form is the line's
+    top-level "precision")."""
     return {
         "workload": "topo, 1 frame: 8,000 charges, 100,000 seeded uniform start points, half-width 1.5 A, "
                     "step 0.001 A, cap 6,000 steps, 20x20 (distance 0-5.2 A, curvature 0-max) histogram",
         "n_charges": N_CHARGES, "n_lines": N_LINES, "half_width_A": HALF, "step_A": STEP, "cap": CAP,
-        "histogram": [20, 20], "precision": precision,
-        "precision_detail": "FP32 pair terms, Kahan across charge tiles, TwoSum warp reduction; "
-                            "FP64 positions, box test, curvature and distance",
+        "histogram": [20, 20],
         "l2": "flushed between timed steps (256 MiB device write)",
     }
+
+
+PRECISION_DETAIL = ("FP32C: FP32 pair terms, Kahan across charge tiles, TwoSum warp reduction; "
+                    "FP64 positions, box test, curvature and distance")
+# CPU legs (our cpu_baseline and the --impl reference arm) time the same sample:
+# every CPU_STRIDE-th line of the 100,000, all of it in one call, the lines
+# spread over all host threads by an atomic counter (the oracle's _mt driver).
+CPU_STRIDE = 100
+
+
+def cpu_sample(starts, caps):
+    idx = np.arange(0, len(starts), CPU_STRIDE)
+    return starts[idx], caps[idx]
 
 
 def make_inputs(rank: int):
@@ -115,55 +128,64 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
-def cpu_baseline(x, q, starts, caps, budget_s=12.0, threads=None):
-    """The oracle's restatement of the reference's float arithmetic
-    (thread_operation, math_module.c:523-591) on all host cores, over the
-    first lines of the same workload until `budget_s` seconds have passed."""
+def cpu_pass(x, q, st, cp, threads):
+    """One pass of the reference's float arithmetic (the oracle's restatement
+    of thread_operation, math_module.c:523-591) over the sample lines."""
     from oracle import oracle
 
+    t0 = time.perf_counter()
+    _, _, steps = oracle.topo_lines_f32(st, cp, x, q, STEP, [HALF] * 3, threads=threads)
+    return time.perf_counter() - t0, steps
+
+
+def cpu_baseline(x, q, starts, caps, min_s=10.0, threads=None):
+    """The CPU leg of this arm: the sample of cpu_sample() on all host cores,
+    repeated until at least `min_s` seconds have passed."""
     threads = threads or os.cpu_count() or 1
-    chunk = 2 * threads
-    done, t0, steps_all = 0, time.perf_counter(), []
-    while done < len(starts) and time.perf_counter() - t0 < budget_s:
-        sl = slice(done, done + chunk)
-        _, _, steps = oracle.topo_lines_f32(starts[sl], caps[sl], x, q, STEP, [HALF] * 3, threads=threads)
-        steps_all.append(steps)
-        done += len(steps)
-    dt = time.perf_counter() - t0
-    steps = np.concatenate(steps_all)
-    return {"lines": done, "seconds": dt, "streamlines_per_s": done / dt,
-            "pair_evals_per_s": pair_evals(steps, len(q)) / dt, "cores": threads}
+    st, cp = cpu_sample(starts, caps)
+    total, passes, steps = 0.0, 0, None
+    while total < min_s or passes == 0:
+        dt, steps = cpu_pass(x, q, st, cp, threads)
+        total += dt
+        passes += 1
+    return {"lines": len(st) * passes, "seconds": total, "streamlines_per_s": len(st) * passes / total,
+            "pair_evals_per_s": pair_evals(steps, len(q)) * passes / total, "cores": threads, "passes": passes}
+
+
+def cpu_sample_text(n):
+    return (f"every {CPU_STRIDE}th of the 100,000 lines ({n} lines, same frame, starts and caps) per pass, "
+            "one call spreading lines over all host threads; the oracle's restatement of the reference's "
+            "float C (thread_operation)")
 
 
 def run_reference(args, world):
     """--impl reference: the reference's CPU implementation of the path (the
     oracle's port of its float C; the reference library itself cannot be
-    built on this host) timed on the host cores, a bounded sample per step."""
+    built on the GPU host) timed on the host cores: each step is one pass over
+    the same strided sample the other arm's cpu_baseline times."""
     from oracle import oracle
 
     oracle.lib()
     x, q, starts, caps = make_inputs(0)
     threads = os.cpu_count() or 1
-    sample = 8 * threads
-    st, sl = starts[:sample], caps[:sample]
+    st, cp = cpu_sample(starts, caps)
     times, pe = [], 0
     for i in range(args.warmup + args.steps):
-        t0 = time.perf_counter()
-        _, _, steps = oracle.topo_lines_f32(st, sl, x, q, STEP, [HALF] * 3, threads=threads)
-        dt = time.perf_counter() - t0
+        dt, steps = cpu_pass(x, q, st, cp, threads)
         if i >= args.warmup:
             times.append(dt)
             pe = pair_evals(steps, len(q))
     total = sum(times)
-    value = sample * len(times) / total
+    value = len(st) * len(times) / total
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": "streamlines/s", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * total / len(times),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
-        "data": "synthetic (seeded; no dataset ships with the benchmark)", "config": workload_config("reference f32"),
+        "data": "synthetic (seeded; no dataset ships with the benchmark)", "config": workload_config(),
+        "precision": "reference float arithmetic (float storage and sums, double pow/sqrt)",
         "pair_evals_per_s": pe * len(times) / total,
         "cpu_baseline": {"value": value, "unit": "streamlines/s", "cores": threads, "kind": "port",
-                         "sample": f"first {sample} of the 100,000 lines per step (same frame, starts, caps)"},
+                         "sample": cpu_sample_text(len(st))},
         "e2e": {"value": value, "unit": "streamlines/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
@@ -251,7 +273,9 @@ def main():
 
     for _ in range(args.warmup):
         step()
-    ffma = _lib.measure_peak(0)  # FP32 pipe peak of this GPU, measured now
+    # FP32 pipe peak of this GPU, measured now: the higher of scalar FFMA and packed FFMA2
+    ffma_scalar, ffma2 = _lib.measure_peak(0), _lib.measure_peak(3)
+    ffma = max(ffma_scalar, ffma2)
     loop_rate = _lib.measure_peak(4)  # the sweep's inner loop alone (pair evaluations/s)
     torch.cuda.synchronize()
 
@@ -296,7 +320,8 @@ def main():
         "warmup": args.warmup, "ms_per_step": 1e3 * total_s / args.steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic (seeded; no dataset ships with the benchmark)",
-        "config": dict(workload_config("fp32c"), n_lines=n_lines),
+        "config": dict(workload_config(), n_lines=n_lines),
+        "precision": "fp32c", "precision_detail": PRECISION_DETAIL,
         "pair_evals_per_s": pe_per_s,
         "latency_ms": {"p50": float(np.percentile(step_ms, 50)), "p99": float(np.percentile(step_ms, 99))},
         "roofline": {"bound": "fp32", "achieved": achieved / 1e12, "peak": ffma / 1e12, "unit": "TFLOP/s",
@@ -308,38 +333,47 @@ def main():
                      "frac_of_sweep_loop": (pe_step / avg_kern_s) / loop_rate,
                      "kernel": "topo_kernel (FP32C, charges resident in shared memory)",
                      "work": f"{FLOPS_PER_PAIR} flop per pair evaluation x sum_lines N*(max(s,2)+2)",
-                     "peak_source": "FFMA throughput measured in this run (cpetgb_measure_peak); "
+                     "peak_source": "FP32 pipe measured in this run (cpetgb_measure_peak): the higher of "
+                                    f"FFMA {ffma_scalar / 1e12:.1f} and packed FFMA2 {ffma2 / 1e12:.1f} TFLOP/s; "
                                     "MEASURED_PEAKS.json holds HBM and bf16 figures only"},
         "gpu_launches": 4 * args.steps,
         "clocks": clocks,
     }
 
     if rank == 0:
-        # e2e: the same step through the C ABI with host buffers in pinned memory
+        # e2e: the same step through the C ABI with host buffers in pinned memory,
+        # every one of the --steps repetitions timed
         pin = lambda a: torch.from_numpy(np.ascontiguousarray(a)).pin_memory().numpy()
         h_starts, h_caps, h_x, h_q = pin(starts), pin(caps), pin(x), pin(q)
         topo_lines(h_starts[:1024], h_caps[:1024], h_x, h_q, STEP, [HALF] * 3, precision="fp32c")
         e2e_t = []
-        for _ in range(max(1, min(args.steps, 3))):
+        for _ in range(args.steps):
             t0 = time.perf_counter()
             r = topo_lines(h_starts, h_caps, h_x, h_q, STEP, [HALF] * 3, precision="fp32c")
             c = topo_hist2d(r, bins=(20, 20), range=hist_range)
             e2e_t.append(time.perf_counter() - t0)
+        # in: starts, caps, charges; the histogram call uploads the (L,2) result again
         h2d = h_starts.nbytes + h_caps.nbytes + h_x.nbytes + h_q.nbytes + r.nbytes
-        d2h = r.nbytes + c.nbytes + 8 * 42
-        out["e2e"] = {"value": n_lines / statistics.median(e2e_t), "unit": "streamlines/s",
+        d2h = r.nbytes + c.nbytes + 8 * 42       # result, counts, bin edges
+        out["e2e"] = {"value": n_lines * len(e2e_t) / sum(e2e_t), "unit": "streamlines/s",
                       "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
-                      "path": "cpetgb_topo_lines + cpetgb_topo_hist2d, CPETGB_HOST, pinned buffers"}
+                      "steps": len(e2e_t),
+                      "path": "cpetgb_topo_lines then cpetgb_topo_hist2d, CPETGB_HOST, pinned buffers "
+                              "(the histogram call copies the result back in)"}
         if not args.no_extras and world == 1:
-            out.update(extras(d_starts, d_caps, d_x, d_q, torch, topo_lines, GridBatch))
-            out["cpu_baseline"] = {}
+            dfma = _lib.measure_peak(1)
+            out.update(extras(d_starts, d_caps, d_x, d_q, torch, topo_lines, GridBatch, dfma))
+            tb = topo_batch_measure(rank, world, dev, torch, dist, 32, 0.1, steps=1, warmup=1)
+            out["topo_batch"] = tb
+            frames, serving = serve_measure(rank, world, torch, dist, 400, 200.0)
+            out["serving"] = dict(serving, config=dict(SERVE_CONFIG, rate_hz=200.0))
+            out["streamline_throughput"] = engine_throughput(frames, rank, torch)
             cb = cpu_baseline(x, q, starts, caps)
             out["cpu_baseline"] = {"value": cb["streamlines_per_s"], "unit": "streamlines/s",
                                    "cores": cb["cores"], "kind": "port",
                                    "pair_evals_per_s": cb["pair_evals_per_s"],
-                                   "sample": f"first {cb['lines']} lines of the same workload "
-                                             f"({cb['seconds']:.1f} s), oracle restatement of the "
-                                             "reference's float C, all host threads"}
+                                   "sample": cpu_sample_text(cb["lines"] // cb["passes"]) +
+                                             f"; {cb['passes']} passes, {cb['seconds']:.1f} s"}
         print(json.dumps(out), flush=True)
     if world > 1:
         dist.destroy_process_group()
@@ -458,31 +492,30 @@ def engine_throughput(frames, rank, torch, n_req=100):
     return out
 
 
-def serve_main(args, rank, world, dev, torch, dist):
-    """--workload serve: Poisson arrivals mixing point_field (1-64 points),
-    volume / volume_ESP (11^3-51^3) and topo requests on resident frames of
-    2,000-100,000 charges; continuous batching; p50/p99 latency per kind.
-    Streamline requests carry 10-500 lines (the serving config's 10^4-10^6 would
-    offer ~10^3 times the device's capacity at 200 requests/s and measure only
-    queueing), so the latency reflects service time at a sustainable load."""
+SERVE_FRAME_SIZES = [2000, 5000, 10000, 20000, 40000, 60000, 80000, 100000]
+
+
+def serve_measure(rank, world, torch, dist, n_requests, rate, fp64_requests=24):
+    """Serving loop (config: Poisson arrivals mixing point_field 1-64 points,
+    volume / volume_ESP 11^3-51^3 and topo requests on resident frames of
+    2,000-100,000 charges; continuous batching): p50/p99 latency per kind for
+    FP32C at `rate` requests/s and FP64 at a 50x lower rate.  Streamline
+    requests carry 10-500 lines (the config's 10^4-10^6 would offer ~10^3 times
+    the device's capacity at 200 requests/s and measure only queueing)."""
     from pycpet_gb300.serving import Server, latency_stats, synthetic_schedule
     from pycpet_gb300.synth import make_frame
 
-    out = {"metric": METRIC, "unit": "requests/s", "n_gpus": world, "steps": 1, "warmup": args.warmup,
-           "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
-           "data": "synthetic (seeded)"}
-    frame_sizes = [2000, 5000, 10000, 20000, 40000, 60000, 80000, 100000]
-    frames = {i: make_frame(n, 600 + i + 100 * rank) for i, n in enumerate(frame_sizes)}
+    frames = {i: make_frame(n, 600 + i + 100 * rank) for i, n in enumerate(SERVE_FRAME_SIZES)}
     results = {}
     # FP64 runs a smaller mix at a lower rate: its pipe is ~75x narrower on this GPU
-    for prec, n_req, rate in (("fp32c", args.requests, args.rate), ("fp64", 24, args.rate / 50)):
+    for prec, n_req, r_hz in (("fp32c", n_requests, rate), ("fp64", fp64_requests, rate / 50)):
         lines = (10, 500)
         srv = Server(precision=prec, line_capacity=4_000_000, charge_capacity=400_000, max_requests=8192)
         for fid, fr in frames.items():
             srv.add_frame(fid, fr["x"], fr["q"])
         warm = synthetic_schedule(list(frames), 8, 1e6, seed=99, topo_lines=(100, 1000))
         srv.run(warm)
-        sched = synthetic_schedule(list(frames), n_req, rate, seed=rank, topo_lines=lines)
+        sched = synthetic_schedule(list(frames), n_req, r_hz, seed=rank, topo_lines=lines)
         if world > 1:
             dist.barrier()
         t0 = time.perf_counter()
@@ -493,19 +526,31 @@ def serve_main(args, rank, world, dev, torch, dist):
         for r in sched:
             n = len(frames[r.frame]["q"])
             pe += (len(r.points) if r.points is not None else 0) * n
-        stats = latency_stats(sched)
-        results[prec] = {"requests": n_req, "rate_hz": rate, "topo_lines": list(lines), "wall_s": wall,
-                         "requests_per_s": n_req / wall,
-                         "grid_pair_evals": pe, "latency": stats,
+        results[prec] = {"requests": n_req, "rate_hz": r_hz, "topo_lines": list(lines), "wall_s": wall,
+                         "requests_per_s": n_req / wall, "completed": sum(r.status == "done" for r in sched),
+                         "grid_pair_evals": pe, "latency": latency_stats(sched),
                          "max_topo_requests_in_flight": srv.max_topo_inflight}
         srv.close()
+    return frames, results
+
+
+SERVE_CONFIG = {"workload": "serving: Poisson arrivals, point_field 1-64 points, volume / volume_ESP "
+                            "11^3-51^3, topo 10-500 lines (step 0.001 A, cap 6,000), frames of "
+                            "2,000-100,000 charges resident on the device",
+                "admission": "80% HBM budget; engine line store 4e6 lines"}
+
+
+def serve_main(args, rank, world, dev, torch, dist):
+    """--workload serve: the serving loop at --rate requests/s (serve_measure)
+    and the engine's streamline throughput (engine_throughput)."""
+    out = {"metric": METRIC, "unit": "requests/s", "n_gpus": world, "steps": 1, "warmup": args.warmup,
+           "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+           "data": "synthetic (seeded)"}
+    frames, results = serve_measure(rank, world, torch, dist, args.requests, args.rate)
     out["streamline_throughput"] = engine_throughput(frames, rank, torch)
     out["value"] = results["fp32c"]["requests_per_s"]
     out["ms_per_step"] = 1e3 * results["fp32c"]["wall_s"]
-    out["config"] = {"workload": f"serving: Poisson arrivals at {args.rate:g}/s, point_field 1-64 points, "
-                                 "volume / volume_ESP 11^3-51^3, topo 10-500 lines (step 0.001 A, cap 6,000), "
-                                 "frames of 2,000-100,000 charges resident on the device",
-                     "admission": "80% HBM budget; engine line store 4e6 lines"}
+    out["config"] = dict(SERVE_CONFIG, rate_hz=args.rate)
     out["serving"] = results
     out["latency_ms"] = {"p50": results["fp32c"]["latency"]["all"]["p50_ms"],
                          "p99": results["fp32c"]["latency"]["all"]["p99_ms"]}
@@ -798,32 +843,32 @@ def dipole_main(args, rank, world, dev, torch, dist):
         dist.destroy_process_group()
 
 
-def topo_batch_main(args, rank, world, dev, torch, dist):
-    """--workload topo-batch: frames of 5,000-20,000 charges (density kept),
-    100,000-1,000,000 lines per frame scaled by --line-scale, half-width 1.5 A,
-    step 0.001 A, cap 6,000; all frames in one persistent launch (FP32C)."""
+def topo_batch_measure(rank, world, dev, torch, dist, n_frames, line_scale, steps, warmup):
+    """Batched topo (config: frames of 5,000-20,000 charges, density kept,
+    100,000-1,000,000 lines per frame scaled by `line_scale`, half-width 1.5 A,
+    step 0.001 A, cap 6,000): all frames in one persistent launch (FP32C).
+    Returns a dict of streamlines/s, pair evaluations/s and per-launch times."""
     from pycpet_gb300 import _lib
     from pycpet_gb300.core import TopoBatch
     from pycpet_gb300.synth import make_frame, random_start_points
 
     rng = np.random.default_rng(3030 + rank)
-    n_frames = args.frames if args.frames != 64 else 32
     frames = []
     for f in range(n_frames):
         n = int(rng.integers(5000, 20001))
-        L = max(1, int(rng.integers(100_000, 1_000_001) * args.line_scale))
+        L = max(1, int(rng.integers(100_000, 1_000_001) * line_scale))
         fr = make_frame(n, seed=7000 + f + 100 * rank)
         frames.append({"x": fr["x"], "q": fr["q"], "starts": random_start_points(L, [HALF] * 3, 8000 + f),
                        "n_iter": CAP, "step": STEP, "half_dims": [HALF] * 3})
     tb = TopoBatch(frames, precision="fp32c", device=True)
-    res, steps = tb.run(return_steps=True)
+    res, stp = tb.run(return_steps=True)
     torch.cuda.synchronize()
-    steps = steps.cpu().numpy()
-    pe = sum(pair_evals(s, len(fr["q"])) for fr, s in zip(frames, tb.split(steps)))
-    for _ in range(args.warmup - 1):
+    stp = stp.cpu().numpy()
+    pe = sum(pair_evals(s_, len(fr["q"])) for fr, s_ in zip(frames, tb.split(stp)))
+    for _ in range(warmup - 1):
         tb.run()
     stream = torch.cuda.current_stream(dev)
-    evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
     if world > 1:
         dist.barrier()
     torch.cuda.synchronize()
@@ -837,25 +882,35 @@ def topo_batch_main(args, rank, world, dev, torch, dist):
     _lib.check(_lib.lib().cpetgb_synchronize(stream.cuda_stream))
     ms = [a.elapsed_time(b) for a, b in evs]
     total_s = sum(ms) * 1e-3
-    out = {"metric": METRIC, "value": tb.n_lines * world * args.steps / total_s, "unit": "streamlines/s",
-           "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * total_s / args.steps,
-           "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
-           "data": "synthetic (seeded)",
-           "config": {"workload": f"batched topo, {n_frames} frames of 5,000-20,000 charges, "
-                                  f"{args.line_scale:g} x (100,000-1,000,000) lines per frame, one launch",
-                      "n_lines": tb.n_lines, "precision": "fp32c"},
-           "pair_evals_per_s": pe * world * args.steps / total_s,
-           "latency_ms": {"p50": float(np.percentile(ms, 50)), "p99": float(np.percentile(ms, 99))}}
+    return {"frames": n_frames, "line_scale": line_scale, "n_lines": tb.n_lines, "steps": steps,
+            "streamlines_per_s": tb.n_lines * steps / total_s, "pair_evals_per_s": pe * steps / total_s,
+            "ms": {"p50": float(np.percentile(ms, 50)), "p99": float(np.percentile(ms, 99))},
+            "workload": f"batched topo, {n_frames} frames of 5,000-20,000 charges, "
+                        f"{line_scale:g} x (100,000-1,000,000) lines per frame, one launch"}
+
+
+def topo_batch_main(args, rank, world, dev, torch, dist):
+    """--workload topo-batch: topo_batch_measure with --frames (default 32) and --line-scale."""
+    n_frames = args.frames if args.frames != 64 else 32
+    r = topo_batch_measure(rank, world, dev, torch, dist, n_frames, args.line_scale, args.steps, args.warmup)
+    out = {"metric": METRIC, "value": r["streamlines_per_s"] * world, "unit": "streamlines/s",
+           "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+           "ms_per_step": r["ms"]["p50"], "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+           "dtype": "f32", "data": "synthetic (seeded)",
+           "config": {"workload": r["workload"], "n_lines": r["n_lines"], "line_scale": args.line_scale},
+           "precision": "fp32c",
+           "pair_evals_per_s": r["pair_evals_per_s"] * world,
+           "latency_ms": r["ms"]}
     if rank == 0:
         print(json.dumps(out), flush=True)
     if world > 1:
         dist.destroy_process_group()
 
 
-def extras(d_starts, d_caps, d_x, d_q, torch, topo_lines, GridBatch):
+def extras(d_starts, d_caps, d_x, d_q, torch, topo_lines, GridBatch, dfma):
     """FP64 plain form on a subset of the same lines (same subset in FP32C for
     the speed-up), and the batched volume/ESP grid workload in both forms."""
-    from pycpet_gb300 import topo_hist2d
+    from pycpet_gb300 import set_field_refinement, topo_hist2d
 
     n_sub = 16384
     res, outs = {}, {}
@@ -880,6 +935,10 @@ def extras(d_starts, d_caps, d_x, d_q, torch, topo_lines, GridBatch):
     curv_rel = np.abs(r32[:, 1] - r64[:, 1]) / np.maximum(np.abs(r64[:, 1]), 1e-300)
     topo_cmp = {"sample": f"first {n_sub} lines", "fp32c": res["fp32c"], "fp64": res["fp64"],
                 "speedup_fp32c_vs_fp64": res["fp64"]["seconds"] / res["fp32c"]["seconds"],
+                "fp64_roofline": {"achieved_tflops": res["fp64"]["pair_evals_per_s"] * FLOPS_PER_PAIR / 1e12,
+                                  "peak_tflops": dfma / 1e12,
+                                  "frac": res["fp64"]["pair_evals_per_s"] * FLOPS_PER_PAIR / dfma,
+                                  "peak_source": "DFMA throughput measured in this run"},
                 "error_fp32c_vs_fp64": {
                     "endpoint_A": {"p50": float(np.median(end_err)), "p99": float(np.quantile(end_err, 0.99)),
                                    "max": float(end_err.max())},
@@ -907,6 +966,22 @@ def extras(d_starts, d_caps, d_x, d_q, torch, topo_lines, GridBatch):
             s = e0.elapsed_time(e1) * 1e-3
             grid[f"{kind}_{prec}"] = {"pair_evals_per_s": gb.pair_evals / s, "ms": s * 1e3}
             vals[prec] = [o.copy() for o in gb.split(out.cpu().numpy())]
+            if kind == "field" and prec == "fp32c":
+                # the same launch without the FP64 refinement of ill-conditioned points
+                tau = set_field_refinement(0.0)
+                gb.run()
+                torch.cuda.synchronize()
+                e0.record()
+                raw = gb.run()
+                e1.record()
+                torch.cuda.synchronize()
+                s0 = e0.elapsed_time(e1) * 1e-3
+                set_field_refinement(tau)
+                refined = int(np.sum(np.any(raw.cpu().numpy() != out.cpu().numpy(), axis=1)))
+                grid["field_fp32c"]["refinement"] = {
+                    "threshold": tau, "points_refined": refined, "ms_without": s0 * 1e3,
+                    "pair_evals_per_s_without": gb.pair_evals / s0,
+                    "rule": "points with |E| < threshold x the frame's median |E| recomputed in IEEE double"}
             del gb
         # FP32C error against the FP64 form (itself within 1e-11 of the CPU FP64 oracle), per frame
         worst_rel, worst_norm, rels = 0.0, 0.0, []

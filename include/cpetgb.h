@@ -302,6 +302,15 @@ int cpetgb_prepare_frame(int mem, int n_atoms, const double* x, const double* q,
  * CPETGB_ERANGE.  Synchronous: waits for `stream` to read the length. */
 int cpetgb_format_fixed3(int mem, int64_t n_rows, int n_cols, const float* values, char* text,
                          int64_t capacity, int64_t* length, void* stream);
+/* The .top writer of the topology dispatcher (np.savetxt(path, hist),
+ * CPET/source/CPET.py:119-123; numpy's default fmt "%.18e"): the rows of a
+ * float32 matrix with every value printed to 19 significant digits, correctly
+ * rounded from its exact binary value, ties to even, as Python formats it
+ * ("nan", "inf", "-inf"; signed zeros kept); single spaces; "\n" after each
+ * row.  At most 26 bytes per value.  Arguments and return as
+ * cpetgb_format_fixed3. */
+int cpetgb_format_sci18(int mem, int64_t n_rows, int n_cols, const float* values, char* text,
+                        int64_t capacity, int64_t* length, void* stream);
 
 /* ---- clustering front end: histograms and distance matrices -------------- */
 /* Histograms of many (distance, curvature) sets with one binning, in one

@@ -82,6 +82,7 @@ SIGNATURES = {
     "cpetgb_topo_hist2d": [_i, _i, _vp, _i, _i, _vp, _vp, _vp, _vp],
     "cpetgb_prepare_frame": [_i, _i, _vp, _vp, _vp, _vp, _vp, _vp, _d, _vp, _vp, _vp, _vp, _vp, _vp],
     "cpetgb_format_fixed3": [_i, ctypes.c_int64, _i, _vp, _vp, ctypes.c_int64, _vp, _vp],
+    "cpetgb_format_sci18": [_i, ctypes.c_int64, _i, _vp, _vp, ctypes.c_int64, _vp, _vp],
     "cpetgb_topo_hist2d_sets": [_i, _i, _vp, _vp, _i, _i, _vp, _vp, _vp, _vp],
     "cpetgb_chi2_distance_matrix": [_i, _i, _i, _i, _vp, _vp, _vp],
     "cpetgb_field_distance_matrix": [_i, _i, _i, _i, _vp, _vp, _vp],

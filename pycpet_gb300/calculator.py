@@ -18,6 +18,7 @@ Streamline post-processing and histograms:
   make_histograms                            calculator.py:596-718  (GPU binning, one launch)
 Output (GPU text formatting):
   save_numpy_as_dat                          CPET/utils/io.py:50-109
+  savetxt (the .top writer)                  numpy.savetxt as called at CPET/source/CPET.py:123
 Clustering front end (GPU distance matrices):
   distance_numpy                             calculator.py:975-978  (numpy, per pair)
   construct_distance_matrix                  calculator.py:1003-1015
@@ -33,7 +34,7 @@ import numpy as np
 
 from . import _lib
 from .c_ops import Math_ops
-from .core import chi2_distance_matrix, field_distance_matrix, format_fixed3, topo_hist2d_sets
+from .core import chi2_distance_matrix, field_distance_matrix, format_fixed3, format_sci18, topo_hist2d_sets
 
 log = logging.getLogger(__name__)
 
@@ -278,6 +279,27 @@ def save_numpy_as_dat(meta_data, volume, name):
     with open(name, "wb") as fh:
         fh.write(header.encode())
         fh.write(body)
+
+
+def savetxt(fname, X, *args, **kwargs):
+    """numpy.savetxt, with the default call numpy.savetxt(fname, X) -- how the
+    topology dispatcher writes every .top file (CPET/source/CPET.py:123) --
+    formatted on the GPU for float32 matrices (the (L,2) streamline results):
+    the same bytes, "%.18e" values joined by spaces, one row per line.  Any
+    other dtype or argument goes to numpy.savetxt itself."""
+    a = np.asarray(X)
+    if args or kwargs or a.dtype != np.float32 or a.ndim not in (1, 2):
+        return np.savetxt(fname, X, *args, **kwargs)
+    body = format_sci18(a.reshape(-1, 1) if a.ndim == 1 else a)
+    if hasattr(fname, "write"):
+        try:
+            fname.write(body)
+        except TypeError:
+            fname.write(body.decode("latin-1"))
+        return None
+    with open(fname, "wb") as fh:
+        fh.write(body)
+    return None
 
 
 def _precision(p):

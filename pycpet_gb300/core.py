@@ -516,6 +516,29 @@ def format_fixed3(values) -> bytes:
     return buf.raw[:length.value]
 
 
+def format_sci18(values) -> bytes:
+    """Rows of a float32 matrix as numpy.savetxt(fname, X) writes them with
+    its default fmt "%.18e" (the .top files of the topology dispatcher,
+    CPET/source/CPET.py:123), formatted on the GPU (cpetgb_format_sci18):
+    every value exactly rounded to 19 significant digits, single spaces, "\n"
+    after each row."""
+    import ctypes
+
+    v = np.asarray(values)
+    if v.dtype != np.float32:
+        raise TypeError("format_sci18 formats float32 values exactly; got " + str(v.dtype))
+    cols = int(np.prod(v.shape[1:])) if v.ndim > 1 else 1
+    v = np.ascontiguousarray(v.reshape(v.shape[0] if v.ndim else 1, cols))
+    n, m = v.shape
+    if n == 0:
+        return b""
+    cap = n * m * 26
+    buf = ctypes.create_string_buffer(cap)
+    length = ctypes.c_int64(0)
+    check(lib().cpetgb_format_sci18(HOST, n, m, v.ctypes.data, buf, cap, ctypes.byref(length), None))
+    return buf.raw[:length.value]
+
+
 # ---------------------------------------------------------------------------
 # Frame preparation
 # ---------------------------------------------------------------------------

@@ -709,8 +709,8 @@ int prepare_frame_impl(int mem, int n, const double* x, const double* q, const i
   return CPETGB_OK;
 }
 
-int format_fixed3_impl(int mem, int64_t n_rows, int n_cols, const float* values, char* text,
-                       int64_t capacity, int64_t* length, void* stream) {
+int format_text_impl(int fmt, int mem, int64_t n_rows, int n_cols, const float* values, char* text,
+                     int64_t capacity, int64_t* length, void* stream) {
   if (!valid_mem(mem)) return fail(CPETGB_EINVAL, "bad memory kind %d", mem);
   if (n_rows < 0 || n_cols < 1) return fail(CPETGB_EINVAL, "need n_rows >= 0 and n_cols >= 1");
   if (!length) return fail(CPETGB_EINVAL, "length pointer is NULL");
@@ -729,7 +729,7 @@ int format_fixed3_impl(int mem, int64_t n_rows, int n_cols, const float* values,
   int64_t* scratch = nullptr;
   CK(S.get(&off, size_t(n_rows) + 1), "alloc offsets");
   CK(S.get(&scratch, size_t(fixed3_scan_scratch(n_rows + 1))), "alloc scan scratch");
-  CK(launch_fixed3_offsets(n_rows, n_cols, dv, off, scratch, s), "length pass");
+  CK(launch_text_offsets(fmt, n_rows, n_cols, dv, off, scratch, s), "length pass");
   int64_t total = 0;
   CK(cudaMemcpyAsync(&total, off + n_rows, sizeof(int64_t), cudaMemcpyDeviceToHost, s), "read length");
   CK(cudaStreamSynchronize(s), "stream synchronize");
@@ -739,7 +739,7 @@ int format_fixed3_impl(int mem, int64_t n_rows, int n_cols, const float* values,
                                     (long long)capacity, (long long)total);
   char* dt = text;
   if (mem == CPETGB_HOST) CK(S.get(&dt, size_t(std::max<int64_t>(total, 1))), "alloc text");
-  CK(launch_fixed3_write(n_rows, n_cols, dv, off, dt, s), "write pass");
+  CK(launch_text_write(fmt, n_rows, n_cols, dv, off, dt, s), "write pass");
   if (mem == CPETGB_HOST) {
     if (total) CK(cudaMemcpyAsync(text, dt, size_t(total), cudaMemcpyDeviceToHost, s), "copy text");
     return finish(c, s);
@@ -1195,7 +1195,12 @@ int cpetgb_prepare_frame(int mem, int n_atoms, const double* x, const double* q,
 
 int cpetgb_format_fixed3(int mem, int64_t n_rows, int n_cols, const float* values, char* text,
                          int64_t capacity, int64_t* length, void* stream) {
-  return format_fixed3_impl(mem, n_rows, n_cols, values, text, capacity, length, stream);
+  return format_text_impl(kTextFixed3, mem, n_rows, n_cols, values, text, capacity, length, stream);
+}
+
+int cpetgb_format_sci18(int mem, int64_t n_rows, int n_cols, const float* values, char* text,
+                        int64_t capacity, int64_t* length, void* stream) {
+  return format_text_impl(kTextSci18, mem, n_rows, n_cols, values, text, capacity, length, stream);
 }
 
 int cpetgb_topo_hist2d_sets(int mem, int n_sets, const int64_t* offsets, const double* values,

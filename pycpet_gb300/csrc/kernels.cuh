@@ -203,12 +203,14 @@ cudaError_t launch_prepare_frame(int n, const double* x, const double* q, const 
 // format.cu: in-place exclusive scan of int64 values (scratch: scan_scratch_i64(n)).
 int64_t scan_scratch_i64(int64_t n);
 cudaError_t scan_exclusive_i64(int64_t n, int64_t* x, int64_t* scratch, cudaStream_t s);
-// format.cu: "%.3f" text of a float32 matrix (numpy.savetxt layout).
+// format.cu: text of a float32 matrix in numpy.savetxt's layout (values joined
+// by single spaces, "\n" after each row), "%.3f" or "%.18e".
+enum TextFormat : int { kTextFixed3 = 0, kTextSci18 = 1 };
 int64_t fixed3_scan_scratch(int64_t n);
-cudaError_t launch_fixed3_offsets(int64_t n_rows, int n_cols, const float* v, int64_t* offsets,
-                                  int64_t* scratch, cudaStream_t s);
-cudaError_t launch_fixed3_write(int64_t n_rows, int n_cols, const float* v, const int64_t* offsets,
-                                char* out, cudaStream_t s);
+cudaError_t launch_text_offsets(int fmt, int64_t n_rows, int n_cols, const float* v,
+                                int64_t* offsets, int64_t* scratch, cudaStream_t s);
+cudaError_t launch_text_write(int fmt, int64_t n_rows, int n_cols, const float* v,
+                              const int64_t* offsets, char* out, cudaStream_t s);
 
 // splits > 1 (distance_splits) needs partial scratch of splits * n * n doubles.
 // FP32C also needs f32_rows scratch of distance_f32_bytes(kind, n, feat) bytes.

@@ -90,17 +90,37 @@ def compute_topo_GPU_batch_filter(self):
     return _topo(self)
 
 
-def patch_pycpet(precision: str = "fp32c"):
+class _NumpyWithGpuSavetxt:
+    """numpy as the dispatcher module sees it, with savetxt formatted on the GPU."""
+
+    def __init__(self, savetxt):
+        self.savetxt = savetxt
+
+    def __getattr__(self, name):
+        return getattr(np, name)
+
+
+def patch_pycpet(precision: str = "fp32c", gpu_writers: bool = False):
     """Route an installed PyCPET's calculator hot-path methods to the GPU.
 
-    Returns the patched class.  Everything else of PyCPET (file parsing,
-    filters, frames, output writers, clustering) is unchanged."""
+    Returns the patched class.  With ``gpu_writers`` the dispatcher's output
+    writers run on the GPU too: save_numpy_as_dat (CPET/source/CPET.py:162,
+    221) and the np.savetxt of .top files (CPET.py:123) in the module
+    CPET.source.CPET, with byte-identical files.  Everything else of PyCPET
+    (file parsing, filters, frames, clustering) is unchanged."""
     from CPET.source import calculator as ref
 
     cls = ref.calculator
     for name in HOT_METHODS:
         setattr(cls, name, globals()[name])
     cls.precision = precision
+    if gpu_writers:
+        from CPET.source import CPET as dispatcher
+
+        from .calculator import save_numpy_as_dat, savetxt
+
+        dispatcher.save_numpy_as_dat = save_numpy_as_dat
+        dispatcher.np = _NumpyWithGpuSavetxt(savetxt)
     return cls
 
 

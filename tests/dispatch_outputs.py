@@ -23,9 +23,10 @@ def fixture_files(g, method):
     return {k[len(pre):]: bytes(g[k]) for k in g.files if k.startswith(pre)}
 
 
-def write_outputs(method, calc, outdir):
-    """The dispatcher's output step for one frame, from `calc`'s methods."""
-    from pycpet_gb300.calculator import save_numpy_as_dat
+def write_outputs(method, calc, outdir, gpu_savetxt=False):
+    """The dispatcher's output step for one frame, from `calc`'s methods
+    (.top files with numpy.savetxt, or with the GPU savetxt drop-in)."""
+    from pycpet_gb300.calculator import save_numpy_as_dat, savetxt
 
     os.makedirs(outdir, exist_ok=True)
     if method == "point_field":
@@ -39,7 +40,8 @@ def write_outputs(method, calc, outdir):
         suffix = "_efield.dat" if method == "volume" else "_esp.dat"
         save_numpy_as_dat(name=os.path.join(outdir, PROTEIN + suffix), volume=box, meta_data=meta)
     else:
-        np.savetxt(os.path.join(outdir, PROTEIN + ".top"), calc.compute_topo_complete_c_shared())
+        (savetxt if gpu_savetxt else np.savetxt)(os.path.join(outdir, PROTEIN + ".top"),
+                                                 calc.compute_topo_complete_c_shared())
     files = {}
     for f in sorted(os.listdir(outdir)):
         with open(os.path.join(outdir, f), "rb") as fh:

@@ -20,8 +20,8 @@ Fixtures written (all small, compressed .npz):
   ref_topo.npz              192 streamlines of a 1,500-charge synthetic frame
                             through the reference's compute_topo_complete_c_shared
   examples_topology.npz     the (distance, curvature) rows of example 3A's
-                            shipped .top files and the reference's
-                            make_histograms of them
+                            shipped .top files, the files' bytes, and the
+                            reference's make_histograms of them
   ref_topo_dipole.npz       160 streamlines of 600 synthetic point dipoles
                             through the reference's
                             compute_topo_complete_c_shared_dipole
@@ -203,6 +203,8 @@ def examples_topology(ref_root, ucalc, out):
     rec = {}
     for i, f in enumerate(files):
         rec[f"top{i}"] = np.loadtxt(f)
+        with open(f, "rb") as fh:
+            rec[f"top{i}_bytes"] = np.frombuffer(fh.read(), dtype=np.uint8)
     rec["hist"] = ucalc.make_histograms(files)
     np.savez_compressed(out, **rec)
 

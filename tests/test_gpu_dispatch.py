@@ -40,3 +40,6 @@ def test_dispatcher_outputs_from_gpu_methods(gpu_lib, golden, tmp_path, precisio
             setattr(calc, name, getattr(drop_in, name).__get__(calc))
         files = D.write_outputs(m, calc, str(tmp_path / precision / m))
         D.compare(m, files, D.fixture_files(g, m))
+        if m == "topo":   # the .top writer on the GPU: numpy's bytes
+            gpu = D.write_outputs(m, calc, str(tmp_path / precision / "gpu_top"), gpu_savetxt=True)
+            assert gpu == files

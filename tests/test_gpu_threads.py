@@ -12,8 +12,8 @@ pytestmark = pytest.mark.gpu
 def test_math_ops_precisions_from_two_threads(gpu_lib, golden):
     from pycpet_gb300.c_ops import Math_ops
 
-    g = golden("ref_grid.npz")
-    t = golden("ref_topo.npz")
+    g = dict(golden("ref_grid.npz"))      # arrays read once: the archive is not thread-safe
+    t = dict(golden("ref_topo.npz"))
     pts = g["mesh"].reshape(-1, 3)
     objs = {"fp64": Math_ops(precision="fp64"), "fp32c": Math_ops(precision="fp32c")}
 
