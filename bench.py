@@ -394,13 +394,13 @@ def grid_main(args, rank, world, dev, torch, dist):
     from pycpet_gb300.core import GridBatch
 
     frames = grid_frames(args.frames, seed=2024 + rank)
-    gbs = [GridBatch(frames, kind=k, precision="fp32c", device=True) for k in ("field", "esp")]
+    gbs = [GridBatch(frames, kind=k, precision="fp32c", device=True, graph=True) for k in ("field", "esp")]
     stream = torch.cuda.current_stream(dev)
     flush = torch.empty(L2_FLUSH_BYTES, dtype=torch.uint8, device=dev)
     for _ in range(args.warmup):
         for gb in gbs:
             gb.run()
-    ffma = _lib.measure_peak(0)
+    ffma = max(_lib.measure_peak(0), _lib.measure_peak(3))  # FP32 pipe: FFMA or packed FFMA2
     evs = [[torch.cuda.Event(enable_timing=True) for _ in range(3)] for _ in range(args.steps)]
     if world > 1:
         dist.barrier()
@@ -424,7 +424,8 @@ def grid_main(args, rank, world, dev, torch, dist):
            "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
            "ms_per_step": 1e3 * total_s / args.steps, "higher_is_better": True, "scaling": "weak",
            "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded)",
-           "config": {"workload": f"batched volume + volume_ESP, {args.frames} frames, FP32C",
+           "config": {"workload": f"batched volume + volume_ESP, {args.frames} frames, FP32C, "
+                                  "one descriptor-table launch per kind captured in a CUDA graph",
                       "pair_evals_per_kind": pe},
            "field_pair_evals_per_s": pe / (statistics.mean(f_ms) * 1e-3),
            "esp_pair_evals_per_s": pe / (statistics.mean(e_ms) * 1e-3),
@@ -951,38 +952,39 @@ def extras(d_starts, d_caps, d_x, d_q, torch, topo_lines, GridBatch, dfma):
 
     # batched volume + volume_ESP: 64 frames, N ~ U[3k, 40k], grids 11^3/21^3/31^3
     frames = grid_frames(64)
-    grid = {}
+    grid = {"pair_evals_per_kind": int(sum(len(p) * len(qq) for p, _, qq in frames))}
+    def timed_plan(kind, prec):
+        """A CUDA-graph plan of the batch (frame table, pack, grid, reduction
+        and refinement kernels), replayed once to warm up and once timed."""
+        gb = GridBatch(frames, kind=kind, precision=prec, device=True, graph=True)
+        gb.run()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        out = gb.run()
+        e1.record()
+        torch.cuda.synchronize()
+        return gb, out.cpu().numpy().copy(), e0.elapsed_time(e1) * 1e-3
+
     for kind in ("field", "esp"):
         vals = {}
         for prec in ("fp32c", "fp64"):
-            gb = GridBatch(frames, kind=kind, precision=prec, device=True)
-            gb.run()
-            torch.cuda.synchronize()
-            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-            e0.record()
-            out = gb.run()
-            e1.record()
-            torch.cuda.synchronize()
-            s = e0.elapsed_time(e1) * 1e-3
-            grid[f"{kind}_{prec}"] = {"pair_evals_per_s": gb.pair_evals / s, "ms": s * 1e3}
-            vals[prec] = [o.copy() for o in gb.split(out.cpu().numpy())]
+            gb, out, s = timed_plan(kind, prec)
+            grid[f"{kind}_{prec}"] = {"pair_evals_per_s": gb.pair_evals / s, "ms": s * 1e3,
+                                      "launch": "CUDA-graph plan (cpetgb_grid_plan_create) replay"}
+            vals[prec] = [o.copy() for o in gb.split(out)]
+            del gb
             if kind == "field" and prec == "fp32c":
                 # the same launch without the FP64 refinement of ill-conditioned points
                 tau = set_field_refinement(0.0)
-                gb.run()
-                torch.cuda.synchronize()
-                e0.record()
-                raw = gb.run()
-                e1.record()
-                torch.cuda.synchronize()
-                s0 = e0.elapsed_time(e1) * 1e-3
+                gb, raw, s0 = timed_plan(kind, prec)
+                del gb
                 set_field_refinement(tau)
-                refined = int(np.sum(np.any(raw.cpu().numpy() != out.cpu().numpy(), axis=1)))
+                refined = int(np.sum(np.any(raw != out, axis=1)))
                 grid["field_fp32c"]["refinement"] = {
                     "threshold": tau, "points_refined": refined, "ms_without": s0 * 1e3,
-                    "pair_evals_per_s_without": gb.pair_evals / s0,
-                    "rule": "points with |E| < threshold x the frame's median |E| recomputed in IEEE double"}
-            del gb
+                    "pair_evals_per_s_without": grid["pair_evals_per_kind"] / s0,
+                    "rule": "points with |E| < threshold x the frame's median |E| recomputed in double-float arithmetic (about 1e-12 per term)"}
         # FP32C error against the FP64 form (itself within 1e-11 of the CPU FP64 oracle), per frame
         worst_rel, worst_norm, rels = 0.0, 0.0, []
         for a, b in zip(vals["fp32c"], vals["fp64"]):
@@ -1000,8 +1002,8 @@ def extras(d_starts, d_caps, d_x, d_q, torch, topo_lines, GridBatch, dfma):
             "max_normwise_rel": worst_norm, "frames": len(frames), "points": int(rels.size),
             "rule": "per point |dE|/|E_ref| (points with |E_ref| < 1e-6 * frame median flagged); normwise "
                     "= max|dE| / max|E_ref| per frame; reference = the FP64 form"}
-    grid["workload"] = "64 frames, 3,000-40,000 charges, 11^3/21^3/31^3 grids, one descriptor-table launch"
-    grid["pair_evals"] = int(sum(len(p) * len(qq) for p, _, qq in frames))
+    grid["workload"] = ("64 frames, 3,000-40,000 charges, 11^3/21^3/31^3 grids, one descriptor-table "
+                        "launch captured in a CUDA graph")
     return {"topo_fp64_vs_fp32c": topo_cmp, "grid_batch": grid}
 
 

@@ -24,7 +24,8 @@
  *     final curvature / distance.  FP32C fields are refined: the points where
  *     |E| is below a fraction (cpetgb_set_field_refinement, default 0.1) of
  *     their frame's median |E| -- where the pair terms cancel and FP32
- *     rounding is largest relative to |E| -- are recomputed in IEEE double.
+ *     rounding is largest relative to |E| -- are recomputed in double-float
+ *     arithmetic (pairs of floats, about 1e-12 relative per pair term).
  */
 #ifndef CPETGB_H
 #define CPETGB_H
@@ -68,8 +69,8 @@ int cpetgb_set_default_precision(int precision);
 int cpetgb_get_default_precision(void);
 /* FP32C field refinement threshold tau in [0, 1] (0 = off; default 0.1):
  * after the FP32C pass, every point of a frame with |E| < tau * (the frame's
- * median |E|, rounded down to 1/16 octave) is recomputed in IEEE double over
- * all of the frame's charges.  Process-wide setting read when a call (or a
+ * median |E|, rounded down to 1/16 octave) is recomputed over all of the
+ * frame's charges in double-float arithmetic (about 1e-12 per pair term).  Process-wide setting read when a call (or a
  * plan, at creation) is made.  No counterpart in the reference, whose field is
  * plain float (CPET/utils/math_module.c:405-451). */
 int cpetgb_set_field_refinement(double tau);

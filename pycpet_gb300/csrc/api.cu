@@ -32,7 +32,7 @@ thread_local std::string g_err;
 std::mutex g_mu;
 std::atomic<int> g_default_prec{CPETGB_FP32C};
 // FP32C field: points with |E| below this fraction of their frame's median |E|
-// are recomputed in IEEE double (0 turns the refinement off).
+// are recomputed in double-float arithmetic (0 turns the refinement off).
 std::atomic<double> g_refine_tau{0.1};
 
 struct Ctx {
@@ -340,11 +340,13 @@ int grid_batch_impl(int kind, int prec, int mem, int clamp, int n_frames, const 
   if (kind == CPETGB_FIELD && prec == CPETGB_FP32C && tau > 0.0 && tot_ch > 0) {
     int64_t *d_desc = nullptr, *list = nullptr;
     int* count = nullptr;
+    unsigned char* dfq = nullptr;
     CK(h2d(&d_desc, S, desc, size_t(n_frames) * 4), "copy frame table");
     CK(S.get(&list, size_t(refine_list_len(n_frames, desc)) * 2), "alloc refinement list");
     CK(S.get(&count, 1), "alloc refinement count");
-    CK(launch_grid_refine(n_frames, d_desc, dp, dx, dq, dout, clamp ? 1 : 0, tau, list, count,
-                          c->sms, s),
+    CK(S.get(&dfq, size_t(tot_ch) * 32), "alloc double-float charges");
+    CK(launch_grid_refine(n_frames, tot_ch, d_desc, dp, dx, dq, dout, clamp ? 1 : 0, tau, list, count,
+                          dfq, c->sms, s),
        "field refinement launch");
   }
   if (mem == CPETGB_HOST) {
@@ -895,8 +897,10 @@ int grid_plan_impl(cpetgb_plan** out_plan, int kind, int prec, int clamp, int n_
   const bool refine = kind == CPETGB_FIELD && prec == CPETGB_FP32C && tau > 0.0 && tot_ch > 0;
   int64_t *d_desc = nullptr, *list = nullptr;
   int* count = nullptr;
+  unsigned char* dfq = nullptr;
   if (refine) {
     e = plan_alloc(pl->bufs, &d_desc, size_t(n_frames) * 4);
+    if (e == cudaSuccess) e = plan_alloc(pl->bufs, &dfq, size_t(tot_ch) * 32);
     if (e == cudaSuccess)
       e = cudaMemcpy(d_desc, desc, size_t(n_frames) * 4 * sizeof(int64_t), cudaMemcpyHostToDevice);
     if (e == cudaSuccess) e = plan_alloc(pl->bufs, &list, size_t(refine_list_len(n_frames, desc)) * 2);
@@ -920,8 +924,8 @@ int grid_plan_impl(cpetgb_plan** out_plan, int kind, int prec, int clamp, int n_
        "grid kernel launch");
     CK(launch_grid_final(kind, n_fin, d_fin, partial, out, cs), "grid reduction launch");
     if (refine)
-      CK(launch_grid_refine(n_frames, d_desc, pts, x, q, out, clamp ? 1 : 0, tau, list, count,
-                            c->sms, cs),
+      CK(launch_grid_refine(n_frames, tot_ch, d_desc, pts, x, q, out, clamp ? 1 : 0, tau, list, count,
+                            dfq, c->sms, cs),
          "field refinement launch");
     return CPETGB_OK;
   });

@@ -31,7 +31,9 @@
 // pair terms (about 1e-7 of each term) is a large fraction of |E|.  After the
 // FP32C pass, grid_flag_kernel finds, per frame, the points whose |E| is below
 // tau times the frame's median |E| and grid_refine_kernel recomputes those
-// points in IEEE double over all of the frame's charges.
+// points over all of the frame's charges in double-float arithmetic (pairs of
+// floats, about 48 significant bits, on the FP32 pipe: GB300's FP64 pipe is
+// 1/64 of its FP32 pipe).
 #include <algorithm>
 #include <type_traits>
 
@@ -470,49 +472,158 @@ __global__ void __launch_bounds__(kFlagThreads)
   }
 }
 
-// Recomputes the listed points in IEEE double: one CTA per point at a time,
-// the frame's charges split over the threads, combined by a fixed tree.
+// Double-float ("float-float") arithmetic: a value is an unevaluated sum
+// h + l of two floats with |l| <= ulp(h)/2, about 48 significant bits, built
+// from the error-free transformations TwoSum (Knuth) and TwoProduct by FMA
+// (Dekker / Kahan; see Muller et al., Handbook of Floating-Point Arithmetic,
+// ch. 4 and 14).  Every operation below is written with explicit roundings
+// (__fadd_rn, __fmul_rn, __fmaf_rn) so the compiler cannot contract or
+// reorder the error terms.
+__device__ __forceinline__ void two_prod(float a, float b, float& p, float& e) {
+  p = __fmul_rn(a, b);
+  e = __fmaf_rn(a, b, -p);
+}
+
+// The field term of one charge at one point in double-float, added to
+// (sh[k], sl[k]).  Point (ph, pl), charge coordinates (ch, cl) and charge
+// (qh, ql) as float pairs.  Relative error of the term about 1e-13.
+template <bool CLAMP>
+__device__ __forceinline__ void df_field_term(const float (&ph)[3], const float (&pl)[3],
+                                              const float4& chq, const float4& clq,
+                                              float (&sh)[3], float (&sl)[3]) {
+  const float ch[3] = {chq.x, chq.y, chq.z}, cl[3] = {clq.x, clq.y, clq.z};
+  float dh[3], dl[3], sq[3], sqe[3];
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    float e;
+    two_sum(ph[k], -ch[k], dh[k], e);                      // dh + e = ph - ch exactly
+    dl[k] = __fadd_rn(e, __fsub_rn(pl[k], cl[k]));
+    {  // renormalise: ph - ch may be exact (e = 0) while pl - cl is not small against it
+      const float h = __fadd_rn(dh[k], dl[k]);
+      dl[k] = __fsub_rn(dl[k], __fsub_rn(h, dh[k]));
+      dh[k] = h;
+    }
+    two_prod(dh[k], dh[k], sq[k], sqe[k]);                 // dh^2 exactly
+    sqe[k] = __fmaf_rn(__fadd_rn(dh[k], dh[k]), dl[k], sqe[k]);  // + 2 dh dl
+  }
+  float t1, e1, r2h, e2;
+  two_sum(sq[0], sq[1], t1, e1);
+  two_sum(t1, sq[2], r2h, e2);
+  float r2l = __fadd_rn(__fadd_rn(e1, e2), __fadd_rn(__fadd_rn(sqe[0], sqe[1]), sqe[2]));
+  {  // renormalise (|r2h| >= |r2l|)
+    const float h = __fadd_rn(r2h, r2l);
+    r2l = __fsub_rn(r2l, __fsub_rn(h, r2h));
+    r2h = h;
+  }
+  if (CLAMP && r2h < 1.0001e-6f) {  // compute_looped_field's r^2 >= 1e-6
+    if (static_cast<double>(r2h) + static_cast<double>(r2l) < 1e-6) {
+      r2h = 1e-6f;
+      r2l = static_cast<float>(1e-6 - static_cast<double>(1e-6f));
+    }
+  }
+  // r^-1: MUFU seed refined by one Newton step with the residual in double-float
+  const float y0 = rsqrt_mufu(r2h);
+  float a, ae, b, be;
+  two_prod(y0, y0, a, ae);                                  // a + ae = y0^2
+  two_prod(r2h, a, b, be);                                  // b + be = r2h a
+  const float t = __fadd_rn(__fsub_rn(b, 1.0f), __fmaf_rn(r2h, ae, __fmaf_rn(r2l, a, be)));
+  const float yl = __fmul_rn(__fmul_rn(-0.5f, y0), t);     // y = y0 + yl
+  // y^3 = (a + (ae + 2 y0 yl)) (y0 + yl)
+  const float y2l = __fmaf_rn(__fadd_rn(y0, y0), yl, ae);
+  float y3h, e3;
+  two_prod(a, y0, y3h, e3);
+  const float y3l = __fmaf_rn(a, yl, __fmaf_rn(y2l, y0, e3));
+  // w = q y^3
+  float wh, e4;
+  two_prod(chq.w, y3h, wh, e4);
+  const float wl = __fmaf_rn(chq.w, y3l, __fmaf_rn(clq.w, y3h, e4));
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    float p, pe, s, se;
+    two_prod(wh, dh[k], p, pe);
+    const float plo = __fmaf_rn(wh, dl[k], __fmaf_rn(wl, dh[k], pe));
+    two_sum(sh[k], p, s, se);
+    sh[k] = s;
+    sl[k] = __fadd_rn(sl[k], __fadd_rn(se, plo));
+  }
+}
+
+// Sum of two double-float values (h, l), renormalised.
+__device__ __forceinline__ void df_add(float& h, float& l, float bh, float bl) {
+  float s, e;
+  two_sum(h, bh, s, e);
+  e = __fadd_rn(e, __fadd_rn(l, bl));
+  h = __fadd_rn(s, e);
+  l = __fsub_rn(e, __fsub_rn(h, s));
+}
+
+// Recomputes the listed points in double-float arithmetic: one CTA per point
+// at a time, the frame's charges (double-float records, pack_df_kernel) split
+// over the threads, the partial sums combined by a fixed tree.
 template <bool CLAMP>
 __global__ void __launch_bounds__(kRefineThreads)
     grid_refine_kernel(const int64_t* __restrict__ desc, const int64_t* __restrict__ list,
                        const int* __restrict__ count, const double* __restrict__ points,
-                       const double* __restrict__ x, const double* __restrict__ q,
-                       double* __restrict__ out) {
-  __shared__ double red[kRefineThreads / 32][3];
+                       const float4* __restrict__ dfq, double* __restrict__ out) {
+  __shared__ float red[kRefineThreads / 32][6];
   const int n_list = *count;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   for (int e = blockIdx.x; e < n_list; e += gridDim.x) {
     const int64_t row = list[2 * e];
     const int64_t f = list[2 * e + 1];
     const int64_t co = desc[4 * f], n = desc[4 * f + 1];
-    const double px = points[3 * row], py = points[3 * row + 1], pz = points[3 * row + 2];
-    double s[3] = {0.0, 0.0, 0.0};
+    float ph[3], pl[3];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+      const double v = points[3 * row + k];
+      ph[k] = __double2float_rn(v);
+      pl[k] = __double2float_rn(v - static_cast<double>(ph[k]));
+    }
+    float sh[3] = {0.f, 0.f, 0.f}, sl[3] = {0.f, 0.f, 0.f};
     for (int64_t j = threadIdx.x; j < n; j += kRefineThreads) {
-      const double* c = x + 3 * (co + j);
-      const double dx = px - c[0], dy = py - c[1], dz = pz - c[2];
-      double r2 = dx * dx + dy * dy + dz * dz;
-      if (CLAMP) r2 = fmax(r2, 1e-6);  // compute_looped_field's clamp
-      const double ri = rsqrt(r2);
-      const double w = (q[co + j] * ri) * (ri * ri);
-      s[0] += w * dx;
-      s[1] += w * dy;
-      s[2] += w * dz;
+      const float4 hi = dfq[2 * (co + j)], lo = dfq[2 * (co + j) + 1];
+      df_field_term<CLAMP>(ph, pl, hi, lo, sh, sl);
     }
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1)
 #pragma unroll
-      for (int a = 0; a < 3; ++a) s[a] += __shfl_xor_sync(0xffffffffu, s[a], o);
+      for (int k = 0; k < 3; ++k) {
+        const float bh = __shfl_xor_sync(0xffffffffu, sh[k], o);
+        const float bl = __shfl_xor_sync(0xffffffffu, sl[k], o);
+        df_add(sh[k], sl[k], bh, bl);
+      }
     if (lane == 0)
 #pragma unroll
-      for (int a = 0; a < 3; ++a) red[warp][a] = s[a];
+      for (int k = 0; k < 3; ++k) {
+        red[warp][2 * k] = sh[k];
+        red[warp][2 * k + 1] = sl[k];
+      }
     __syncthreads();
     if (threadIdx.x < 3) {
-      double v = 0.0;
+      const int k = threadIdx.x;
+      float h = red[0][2 * k], l = red[0][2 * k + 1];
 #pragma unroll
-      for (int w = 0; w < kRefineThreads / 32; ++w) v += red[w][threadIdx.x];
-      out[3 * row + threadIdx.x] = v * kCoulomb;
+      for (int w = 1; w < kRefineThreads / 32; ++w) df_add(h, l, red[w][2 * k], red[w][2 * k + 1]);
+      out[3 * row + k] = (static_cast<double>(h) + static_cast<double>(l)) * kCoulomb;
     }
     __syncthreads();
+  }
+}
+
+// Charges as double-float records {xh, yh, zh, qh} {xl, yl, zl, ql}.
+__global__ void pack_df_kernel(int64_t n, const double* __restrict__ x, const double* __restrict__ q,
+                               float4* __restrict__ out) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    float h[4], l[4];
+    const double v[4] = {x[3 * i], x[3 * i + 1], x[3 * i + 2], q[i]};
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      h[k] = __double2float_rn(v[k]);
+      l[k] = __double2float_rn(v[k] - static_cast<double>(h[k]));
+    }
+    out[2 * i] = make_float4(h[0], h[1], h[2], h[3]);
+    out[2 * i + 1] = make_float4(l[0], l[1], l[2], l[3]);
   }
 }
 
@@ -640,18 +751,22 @@ cudaError_t preload_grid_kernels(int prec, int kind, int clamp, int ppt) {
                         : cudaFuncGetAttributes(&a, pack_f64_kernel);
 }
 
-cudaError_t launch_grid_refine(int n_frames, const int64_t* desc, const double* points,
-                               const double* x, const double* q, double* out, int clamp,
-                               double tau, int64_t* list, int* count, int num_sms, cudaStream_t s) {
-  if (n_frames <= 0 || !(tau > 0.0)) return cudaSuccess;
+cudaError_t launch_grid_refine(int n_frames, int64_t n_charges, const int64_t* desc,
+                               const double* points, const double* x, const double* q, double* out,
+                               int clamp, double tau, int64_t* list, int* count, void* df_charges,
+                               int num_sms, cudaStream_t s) {
+  if (n_frames <= 0 || n_charges <= 0 || !(tau > 0.0)) return cudaSuccess;
   cudaError_t e = cudaMemsetAsync(count, 0, sizeof(int), s);
   if (e != cudaSuccess) return e;
+  float4* dfq = static_cast<float4*>(df_charges);
+  const int pack_blocks = static_cast<int>(std::min<int64_t>((n_charges + 255) / 256, 4096));
+  pack_df_kernel<<<pack_blocks, 256, 0, s>>>(n_charges, x, q, dfq);
   grid_flag_kernel<<<n_frames, kFlagThreads, 0, s>>>(desc, out, tau, list, count);
   const int ctas = std::max(num_sms, 1) * 8;
   if (clamp)
-    grid_refine_kernel<true><<<ctas, kRefineThreads, 0, s>>>(desc, list, count, points, x, q, out);
+    grid_refine_kernel<true><<<ctas, kRefineThreads, 0, s>>>(desc, list, count, points, dfq, out);
   else
-    grid_refine_kernel<false><<<ctas, kRefineThreads, 0, s>>>(desc, list, count, points, x, q, out);
+    grid_refine_kernel<false><<<ctas, kRefineThreads, 0, s>>>(desc, list, count, points, dfq, out);
   return cudaGetLastError();
 }
 
@@ -660,6 +775,7 @@ cudaError_t preload_grid_refine() {
   cudaError_t e = cudaFuncGetAttributes(&a, grid_flag_kernel);
   if (e == cudaSuccess) e = cudaFuncGetAttributes(&a, grid_refine_kernel<true>);
   if (e == cudaSuccess) e = cudaFuncGetAttributes(&a, grid_refine_kernel<false>);
+  if (e == cudaSuccess) e = cudaFuncGetAttributes(&a, pack_df_kernel);
   return e;
 }
 

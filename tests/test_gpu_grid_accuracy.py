@@ -46,8 +46,9 @@ def test_field_fp32c_per_point_on_largest_volume_frames(gpu_lib, oracle):
 
 
 def test_refined_points_equal_fp64(gpu_lib, oracle):
-    """Points below the refinement threshold come out of the FP32C call in
-    IEEE double (within 1e-9 of the oracle per point), the rest unchanged;
+    """Points below the refinement threshold come out of the FP32C call
+    recomputed in double-float arithmetic (within 1e-9 of the oracle per
+    point), the rest unchanged;
     with the refinement off the same call is plain FP32C."""
     from pycpet_gb300 import field_grid, set_field_refinement
     from pycpet_gb300.synth import cube_points, make_frame
