@@ -984,7 +984,8 @@ def extras(d_starts, d_caps, d_x, d_q, torch, topo_lines, GridBatch, dfma):
                 grid["field_fp32c"]["refinement"] = {
                     "threshold": tau, "points_refined": refined, "ms_without": s0 * 1e3,
                     "pair_evals_per_s_without": grid["pair_evals_per_kind"] / s0,
-                    "rule": "points with |E| < threshold x the frame's median |E| recomputed in double-float arithmetic (about 1e-12 per term)"}
+                    "rule": "points with |E| < threshold x the frame's median |E| recomputed in "
+                            "double-float arithmetic (about 1e-12 per term)"}
         # FP32C error against the FP64 form (itself within 1e-11 of the CPU FP64 oracle), per frame
         worst_rel, worst_norm, rels = 0.0, 0.0, []
         for a, b in zip(vals["fp32c"], vals["fp64"]):

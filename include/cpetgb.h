@@ -70,9 +70,10 @@ int cpetgb_get_default_precision(void);
 /* FP32C field refinement threshold tau in [0, 1] (0 = off; default 0.1):
  * after the FP32C pass, every point of a frame with |E| < tau * (the frame's
  * median |E|, rounded down to 1/16 octave) is recomputed over all of the
- * frame's charges in double-float arithmetic (about 1e-12 per pair term).  Process-wide setting read when a call (or a
- * plan, at creation) is made.  No counterpart in the reference, whose field is
- * plain float (CPET/utils/math_module.c:405-451). */
+ * frame's charges in double-float arithmetic (about 1e-12 per pair term).
+ * Process-wide setting read when a call (or a plan, at creation) is made.  No
+ * counterpart in the reference, whose field is plain float
+ * (CPET/utils/math_module.c:405-451). */
 int cpetgb_set_field_refinement(double tau);
 double cpetgb_field_refinement(void);
 
