@@ -271,6 +271,12 @@ int64_t refine_list_len(int n_frames, const int64_t* desc) {
   return std::max<int64_t>(n, 1);
 }
 
+int64_t max_frame_points(int n_frames, const int64_t* desc) {
+  int64_t m = 0;
+  for (int f = 0; f < n_frames; ++f) m = std::max(m, desc[4 * f + 3]);
+  return m;
+}
+
 double grid_pair_evals(int n_frames, const int64_t* desc) {
   double total = 0.0;
   for (int f = 0; f < n_frames; ++f) total += double(desc[4 * f + 1]) * double(desc[4 * f + 3]);
@@ -341,12 +347,14 @@ int grid_batch_impl(int kind, int prec, int mem, int clamp, int n_frames, const 
     int64_t *d_desc = nullptr, *list = nullptr;
     int* count = nullptr;
     unsigned char* dfq = nullptr;
+    int* hist = nullptr;
     CK(h2d(&d_desc, S, desc, size_t(n_frames) * 4), "copy frame table");
     CK(S.get(&list, size_t(refine_list_len(n_frames, desc)) * 2), "alloc refinement list");
     CK(S.get(&count, 1), "alloc refinement count");
+    CK(S.get(&hist, size_t(grid_refine_hist_ints(n_frames))), "alloc magnitude histograms");
     CK(S.get(&dfq, size_t(tot_ch) * 32), "alloc double-float charges");
-    CK(launch_grid_refine(n_frames, tot_ch, d_desc, dp, dx, dq, dout, clamp ? 1 : 0, tau, list, count,
-                          dfq, c->sms, s),
+    CK(launch_grid_refine(n_frames, tot_ch, max_frame_points(n_frames, desc), d_desc, dp, dx, dq, dout,
+                          clamp ? 1 : 0, tau, list, count, hist, dfq, c->sms, s),
        "field refinement launch");
   }
   if (mem == CPETGB_HOST) {
@@ -898,8 +906,10 @@ int grid_plan_impl(cpetgb_plan** out_plan, int kind, int prec, int clamp, int n_
   int64_t *d_desc = nullptr, *list = nullptr;
   int* count = nullptr;
   unsigned char* dfq = nullptr;
+  int* hist = nullptr;
   if (refine) {
     e = plan_alloc(pl->bufs, &d_desc, size_t(n_frames) * 4);
+    if (e == cudaSuccess) e = plan_alloc(pl->bufs, &hist, size_t(grid_refine_hist_ints(n_frames)));
     if (e == cudaSuccess) e = plan_alloc(pl->bufs, &dfq, size_t(tot_ch) * 32);
     if (e == cudaSuccess)
       e = cudaMemcpy(d_desc, desc, size_t(n_frames) * 4 * sizeof(int64_t), cudaMemcpyHostToDevice);
@@ -924,8 +934,8 @@ int grid_plan_impl(cpetgb_plan** out_plan, int kind, int prec, int clamp, int n_
        "grid kernel launch");
     CK(launch_grid_final(kind, n_fin, d_fin, partial, out, cs), "grid reduction launch");
     if (refine)
-      CK(launch_grid_refine(n_frames, tot_ch, d_desc, pts, x, q, out, clamp ? 1 : 0, tau, list, count,
-                            dfq, c->sms, cs),
+      CK(launch_grid_refine(n_frames, tot_ch, max_frame_points(n_frames, desc), d_desc, pts, x, q, out,
+                            clamp ? 1 : 0, tau, list, count, hist, dfq, c->sms, cs),
          "field refinement launch");
     return CPETGB_OK;
   });

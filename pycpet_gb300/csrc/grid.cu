@@ -29,8 +29,9 @@
 //
 // FP32C field refinement: where the field nearly cancels, FP32 rounding of the
 // pair terms (about 1e-7 of each term) is a large fraction of |E|.  After the
-// FP32C pass, grid_flag_kernel finds, per frame, the points whose |E| is below
-// tau times the frame's median |E| and grid_refine_kernel recomputes those
+// FP32C pass, grid_mag_hist_kernel and grid_flag_kernel find, per frame, the
+// points whose |E| is below tau times the frame's median |E| (taken from a
+// histogram of |E|^2) and grid_refine_kernel recomputes those
 // points over all of the frame's charges in double-float arithmetic (pairs of
 // floats, about 48 significant bits, on the FP32 pipe: GB300's FP64 pipe is
 // 1/64 of its FP32 pipe).
@@ -401,37 +402,113 @@ __global__ void grid_final_kernel(const GridFinal* __restrict__ fin,
 // FP32C field refinement (see the header comment).
 // ---------------------------------------------------------------------------
 constexpr int kFlagThreads = 512;
-constexpr int kMagBins = 4096;  // bits 30..19 of the float |E|: exponent + 4 mantissa bits
+constexpr int kFlagChunk = kFlagThreads * 8;  // points of a frame per flagging CTA
+constexpr int kMagBins = 4096;  // bits 30..19 of the float |E|^2: exponent + 4 mantissa bits
 constexpr int kBinsPerThread = kMagBins / kFlagThreads;
-constexpr int kRefineThreads = 256;
+constexpr int kRefineThreads = 1024;
 
-__device__ __forceinline__ double field_norm(const double* e) {
-  return sqrt(e[0] * e[0] + e[1] * e[1] + e[2] * e[2]);
+// Integer-only reads of doubles.  GB300's FP64 pipe is 1/64 of its FP32 pipe
+// and conversions from double run on it, so the refinement's helpers take a
+// double apart with integer operations.
+//   dbl_hi_float: sign, exponent and the leading 24 significand bits (the rest
+//                 truncated); beyond the float range +-inf, below its normal
+//                 range +-0; NaN stays NaN.
+//   dbl_lo_float: the remaining 29 significand bits, v - dbl_hi_float(v),
+//                 rounded to a float (|error| <= 2^-48 |v|); 0 where the high
+//                 part is not a normal float, and flushed to 0 where it would
+//                 be subnormal (|v| below about 1e-30: an absolute error
+//                 under 1e-37).
+__device__ __forceinline__ float dbl_hi_float(double v) {
+  const unsigned long long b = static_cast<unsigned long long>(__double_as_longlong(v));
+  const uint32_t sign = static_cast<uint32_t>(b >> 32) & 0x80000000u;
+  const int ex = static_cast<int>((b >> 52) & 0x7ff);
+  const uint32_t mant = static_cast<uint32_t>((b >> 29) & 0x7fffffu);
+  if (ex == 0x7ff) return __uint_as_float(sign | 0x7f800000u | (mant ? 0x400000u : 0u));
+  const int e = ex - 1023 + 127;
+  if (e >= 255) return __uint_as_float(sign | 0x7f800000u);
+  if (e <= 0) return __uint_as_float(sign);
+  return __uint_as_float(sign | (static_cast<uint32_t>(e) << 23) | mant);
+}
+__device__ __forceinline__ float dbl_lo_float(double v) {
+  const unsigned long long b = static_cast<unsigned long long>(__double_as_longlong(v));
+  const uint32_t sign = static_cast<uint32_t>(b >> 32) & 0x80000000u;
+  const int ex = static_cast<int>((b >> 52) & 0x7ff);
+  const uint32_t r = static_cast<uint32_t>(b & 0x1fffffffull);  // 29 bits, weight 2^(ex - 1075)
+  const int e_hi = ex - 1023 + 127;
+  if (r == 0 || e_hi <= 0 || e_hi >= 255) return 0.f;
+  const int t = 31 - __clz(static_cast<int>(r));  // top set bit, 0..28
+  uint32_t m;
+  int fe = ex - 1075 + t + 127;                   // float exponent of r's top bit
+  if (t > 23) {                                   // round the low t - 23 bits, half up
+    const int sh = t - 23;
+    m = (r >> sh) + ((r >> (sh - 1)) & 1u);
+    if (m == (1u << 24)) {
+      m >>= 1;
+      ++fe;
+    }
+  } else {
+    m = r << (23 - t);
+  }
+  if (fe <= 0) return __uint_as_float(sign);
+  return __uint_as_float(sign | (static_cast<uint32_t>(fe) << 23) | (m & 0x7fffffu));
 }
 
-// One CTA per frame (desc rows {charge_off, n, point_off, P}).  Histograms the
-// frame's |E| in 1/16-octave bins, takes the lower edge of the bin holding the
-// lower median as the frame's scale, and appends every point with |E| below
-// tau times that scale to list[] as {output row, frame}.  The counts are exact
-// integers, so the threshold -- and the set of points -- is deterministic.
+// |E|^2 of one output row in FP32 from the truncated components (integer
+// conversion, three FP32 operations): the key of the magnitude histogram.
+__device__ __forceinline__ float field_norm2(const double* e) {
+  const float x = dbl_hi_float(e[0]), y = dbl_hi_float(e[1]), z = dbl_hi_float(e[2]);
+  return __fmaf_rn(x, x, __fmaf_rn(y, y, __fmul_rn(z, z)));
+}
+
+// Histogram of |E|^2 over the frames' points in 1/16-octave bins (of |E|^2;
+// 1/32 octave of |E|): grid (frame, chunk of kFlagChunk points); each CTA
+// counts its chunk in shared memory and adds its non-empty bins to the frame's
+// row of hist[n_frames][kMagBins] (zeroed by the caller).
 __global__ void __launch_bounds__(kFlagThreads)
-    grid_flag_kernel(const int64_t* __restrict__ desc, const double* __restrict__ out, double tau,
-                     int64_t* __restrict__ list, int* __restrict__ count) {
-  __shared__ int hist[kMagBins];
+    grid_mag_hist_kernel(const int64_t* __restrict__ desc, const double* __restrict__ out,
+                         int* __restrict__ hist) {
+  __shared__ int h[kMagBins];
+  const int64_t po = desc[4 * blockIdx.x + 2], P = desc[4 * blockIdx.x + 3];
+  const int64_t i0 = static_cast<int64_t>(blockIdx.y) * kFlagChunk;
+  if (i0 >= P) return;
+  const int64_t i1 = min(P, i0 + kFlagChunk);
+  for (int b = threadIdx.x; b < kMagBins; b += kFlagThreads) h[b] = 0;
+  __syncthreads();
+  for (int64_t i = i0 + threadIdx.x; i < i1; i += kFlagThreads) {
+    const float m2 = field_norm2(out + 3 * (po + i));
+    if (m2 <= 3.0e38f)  // finite (NaN compares false)
+      atomicAdd(&h[__float_as_uint(m2) >> 19], 1);
+  }
+  __syncthreads();
+  int* row = hist + static_cast<int64_t>(blockIdx.x) * kMagBins;
+  for (int b = threadIdx.x; b < kMagBins; b += kFlagThreads)
+    if (h[b]) atomicAdd(&row[b], h[b]);
+}
+
+// Grid (frame, chunk) as grid_mag_hist_kernel.  Every CTA finds its frame's
+// scale -- the lower edge of the histogram bin holding the lower median of
+// |E|^2 -- and appends each point of its chunk with |E|^2 below tau^2 times
+// that scale to list[] as {output row, frame}.  The counts are exact
+// integers, so the threshold and the set of points are deterministic.
+__global__ void __launch_bounds__(kFlagThreads)
+    grid_flag_kernel(const int64_t* __restrict__ desc, const double* __restrict__ out,
+                     const int* __restrict__ hist, float tau2, int64_t* __restrict__ list,
+                     int* __restrict__ count) {
+  __shared__ int hs[kMagBins];
   __shared__ int part[kFlagThreads];
   __shared__ float scale_s;
   const int64_t po = desc[4 * blockIdx.x + 2], P = desc[4 * blockIdx.x + 3];
-  for (int b = threadIdx.x; b < kMagBins; b += kFlagThreads) hist[b] = 0;
-  __syncthreads();
-  for (int64_t i = threadIdx.x; i < P; i += kFlagThreads) {
-    const double m = field_norm(out + 3 * (po + i));
-    if (m <= 3.0e38)  // finite in float (NaN compares false)
-      atomicAdd(&hist[__float_as_uint(static_cast<float>(m)) >> 19], 1);
-  }
-  __syncthreads();
+  const int64_t i0 = static_cast<int64_t>(blockIdx.y) * kFlagChunk;
+  if (i0 >= P) return;
+  const int64_t i1 = min(P, i0 + kFlagChunk);
+  const int* row = hist + static_cast<int64_t>(blockIdx.x) * kMagBins;
   int own = 0;
 #pragma unroll
-  for (int k = 0; k < kBinsPerThread; ++k) own += hist[threadIdx.x * kBinsPerThread + k];
+  for (int k = 0; k < kBinsPerThread; ++k) {
+    const int v = row[threadIdx.x * kBinsPerThread + k];
+    hs[threadIdx.x * kBinsPerThread + k] = v;
+    own += v;
+  }
   part[threadIdx.x] = own;
   __syncthreads();
   if (threadIdx.x < 32) {
@@ -456,15 +533,15 @@ __global__ void __launch_bounds__(kFlagThreads)
         int cum = incl - mine, t = lane * kPerLane;
         while (cum + part[t] <= rank) cum += part[t++];
         int b = t * kBinsPerThread;
-        while (cum + hist[b] <= rank) cum += hist[b++];
+        while (cum + hs[b] <= rank) cum += hs[b++];
         scale_s = __uint_as_float(static_cast<uint32_t>(b) << 19);
       }
     }
   }
   __syncthreads();
-  const double thr = tau * static_cast<double>(scale_s);
-  for (int64_t i = threadIdx.x; i < P; i += kFlagThreads) {
-    if (field_norm(out + 3 * (po + i)) < thr) {
+  const float thr = __fmul_rn(tau2, scale_s);
+  for (int64_t i = i0 + threadIdx.x; i < i1; i += kFlagThreads) {
+    if (field_norm2(out + 3 * (po + i)) < thr) {
       const int k = atomicAdd(count, 1);
       list[2 * k] = po + i;
       list[2 * k + 1] = blockIdx.x;
@@ -575,9 +652,8 @@ __global__ void __launch_bounds__(kRefineThreads)
     float ph[3], pl[3];
 #pragma unroll
     for (int k = 0; k < 3; ++k) {
-      const double v = points[3 * row + k];
-      ph[k] = __double2float_rn(v);
-      pl[k] = __double2float_rn(v - static_cast<double>(ph[k]));
+      ph[k] = dbl_hi_float(points[3 * row + k]);
+      pl[k] = dbl_lo_float(points[3 * row + k]);
     }
     float sh[3] = {0.f, 0.f, 0.f}, sl[3] = {0.f, 0.f, 0.f};
     for (int64_t j = threadIdx.x; j < n; j += kRefineThreads) {
@@ -615,15 +691,11 @@ __global__ void pack_df_kernel(int64_t n, const double* __restrict__ x, const do
                                float4* __restrict__ out) {
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
        i += (int64_t)gridDim.x * blockDim.x) {
-    float h[4], l[4];
     const double v[4] = {x[3 * i], x[3 * i + 1], x[3 * i + 2], q[i]};
-#pragma unroll
-    for (int k = 0; k < 4; ++k) {
-      h[k] = __double2float_rn(v[k]);
-      l[k] = __double2float_rn(v[k] - static_cast<double>(h[k]));
-    }
-    out[2 * i] = make_float4(h[0], h[1], h[2], h[3]);
-    out[2 * i + 1] = make_float4(l[0], l[1], l[2], l[3]);
+    out[2 * i] = make_float4(dbl_hi_float(v[0]), dbl_hi_float(v[1]), dbl_hi_float(v[2]),
+                             dbl_hi_float(v[3]));
+    out[2 * i + 1] = make_float4(dbl_lo_float(v[0]), dbl_lo_float(v[1]), dbl_lo_float(v[2]),
+                                 dbl_lo_float(v[3]));
   }
 }
 
@@ -751,18 +823,22 @@ cudaError_t preload_grid_kernels(int prec, int kind, int clamp, int ppt) {
                         : cudaFuncGetAttributes(&a, pack_f64_kernel);
 }
 
-cudaError_t launch_grid_refine(int n_frames, int64_t n_charges, const int64_t* desc,
-                               const double* points, const double* x, const double* q, double* out,
-                               int clamp, double tau, int64_t* list, int* count, void* df_charges,
-                               int num_sms, cudaStream_t s) {
-  if (n_frames <= 0 || n_charges <= 0 || !(tau > 0.0)) return cudaSuccess;
+cudaError_t launch_grid_refine(int n_frames, int64_t n_charges, int64_t max_points,
+                               const int64_t* desc, const double* points, const double* x,
+                               const double* q, double* out, int clamp, double tau, int64_t* list,
+                               int* count, int* hist, void* df_charges, int num_sms, cudaStream_t s) {
+  if (n_frames <= 0 || n_charges <= 0 || max_points <= 0 || !(tau > 0.0)) return cudaSuccess;
   cudaError_t e = cudaMemsetAsync(count, 0, sizeof(int), s);
+  if (e == cudaSuccess) e = cudaMemsetAsync(hist, 0, size_t(n_frames) * kMagBins * sizeof(int), s);
   if (e != cudaSuccess) return e;
   float4* dfq = static_cast<float4*>(df_charges);
   const int pack_blocks = static_cast<int>(std::min<int64_t>((n_charges + 255) / 256, 4096));
   pack_df_kernel<<<pack_blocks, 256, 0, s>>>(n_charges, x, q, dfq);
-  grid_flag_kernel<<<n_frames, kFlagThreads, 0, s>>>(desc, out, tau, list, count);
-  const int ctas = std::max(num_sms, 1) * 8;
+  const dim3 fgrid(n_frames, static_cast<unsigned>((max_points + kFlagChunk - 1) / kFlagChunk));
+  grid_mag_hist_kernel<<<fgrid, kFlagThreads, 0, s>>>(desc, out, hist);
+  const float tau2 = static_cast<float>(tau * tau);
+  grid_flag_kernel<<<fgrid, kFlagThreads, 0, s>>>(desc, out, hist, tau2, list, count);
+  const int ctas = std::max(num_sms, 1) * 2;
   if (clamp)
     grid_refine_kernel<true><<<ctas, kRefineThreads, 0, s>>>(desc, list, count, points, dfq, out);
   else
@@ -770,9 +846,12 @@ cudaError_t launch_grid_refine(int n_frames, int64_t n_charges, const int64_t* d
   return cudaGetLastError();
 }
 
+int64_t grid_refine_hist_ints(int n_frames) { return int64_t(std::max(n_frames, 1)) * kMagBins; }
+
 cudaError_t preload_grid_refine() {
   cudaFuncAttributes a;
   cudaError_t e = cudaFuncGetAttributes(&a, grid_flag_kernel);
+  if (e == cudaSuccess) e = cudaFuncGetAttributes(&a, grid_mag_hist_kernel);
   if (e == cudaSuccess) e = cudaFuncGetAttributes(&a, grid_refine_kernel<true>);
   if (e == cudaSuccess) e = cudaFuncGetAttributes(&a, grid_refine_kernel<false>);
   if (e == cudaSuccess) e = cudaFuncGetAttributes(&a, pack_df_kernel);

@@ -76,14 +76,17 @@ cudaError_t launch_grid_final(int kind, int n_final, const GridFinal* fin,
                               const double* partial, double* out, cudaStream_t s);
 
 // FP32C field refinement after the grid pass: points of each frame (desc rows
-// {charge_off, n, point_off, P}, device memory) whose |E| is below tau times
-// the frame's median |E| are recomputed in double-float arithmetic from x/q
-// (n_charges of them in all).  list holds 2 int64 per point of the launch,
-// count one int (zeroed here), df_charges 32 bytes per charge.  tau <= 0: no-op.
-cudaError_t launch_grid_refine(int n_frames, int64_t n_charges, const int64_t* desc,
-                               const double* points, const double* x, const double* q, double* out,
-                               int clamp, double tau, int64_t* list, int* count, void* df_charges,
-                               int num_sms, cudaStream_t s);
+// {charge_off, n, point_off, P}, device memory; max_points = the largest P)
+// whose |E| is below tau times the frame's median |E| are recomputed in
+// double-float arithmetic from x/q (n_charges of them in all).  Scratch: list
+// 2 int64 per point of the launch, count one int, hist
+// grid_refine_hist_ints(n_frames) ints (both zeroed here), df_charges 32 bytes
+// per charge.  tau <= 0: no-op.
+cudaError_t launch_grid_refine(int n_frames, int64_t n_charges, int64_t max_points,
+                               const int64_t* desc, const double* points, const double* x,
+                               const double* q, double* out, int clamp, double tau, int64_t* list,
+                               int* count, int* hist, void* df_charges, int num_sms, cudaStream_t s);
+int64_t grid_refine_hist_ints(int n_frames);
 cudaError_t preload_grid_refine();
 
 // topo.cu
