@@ -22,7 +22,7 @@
  *     drop-in); CPETGB_FP32C = FP32 pair terms with compensated (Kahan)
  *     accumulation across charge tiles, FP64 for streamline positions and the
  *     final curvature / distance.  FP32C fields are refined: the points where
- *     |E| is below a fraction (cpetgb_set_field_refinement, default 0.1) of
+ *     |E| is below a fraction (cpetgb_set_field_refinement, default 0.15) of
  *     their frame's median |E| -- where the pair terms cancel and FP32
  *     rounding is largest relative to |E| -- are recomputed in double-float
  *     arithmetic (pairs of floats, about 1e-12 relative per pair term).
@@ -67,7 +67,7 @@ int cpetgb_synchronize(void* stream);
  * Process-wide; the *_p variants take the precision per call instead. */
 int cpetgb_set_default_precision(int precision);
 int cpetgb_get_default_precision(void);
-/* FP32C field refinement threshold tau in [0, 1] (0 = off; default 0.1):
+/* FP32C field refinement threshold tau in [0, 1] (0 = off; default 0.15):
  * after the FP32C pass, every point of a frame with |E| < tau * (the frame's
  * median |E|, rounded down to 1/16 octave) is recomputed over all of the
  * frame's charges in double-float arithmetic (about 1e-12 per pair term).

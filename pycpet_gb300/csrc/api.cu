@@ -33,7 +33,7 @@ std::mutex g_mu;
 std::atomic<int> g_default_prec{CPETGB_FP32C};
 // FP32C field: points with |E| below this fraction of their frame's median |E|
 // are recomputed in double-float arithmetic (0 turns the refinement off).
-std::atomic<double> g_refine_tau{0.1};
+std::atomic<double> g_refine_tau{0.15};
 
 struct Ctx {
   bool ready = false;
