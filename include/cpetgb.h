@@ -13,6 +13,12 @@
  *     returns when the results are in place) or CPETGB_DEVICE (device memory of
  *     the current device; the call is enqueued on `stream` and returns at once;
  *     cpetgb_synchronize(stream) waits and reports errors raised on the device).
+ *   - Errors raised inside kernels (a bounded wait that ran out, a refused
+ *     step cap or histogram range) go to one status word per device.  The next
+ *     call that waits on the device -- cpetgb_synchronize or any CPETGB_HOST
+ *     call, on whichever stream -- reports that status and clears it.  To tie
+ *     such an error to the CPETGB_DEVICE call that raised it, call
+ *     cpetgb_synchronize(stream) after that call, before other work.
  *   - `stream` is a cudaStream_t; NULL means the legacy default stream for
  *     CPETGB_DEVICE calls and a library-owned stream for CPETGB_HOST calls.
  *   - Coordinates are in Angstrom, charges in e, fields in V/A, potentials in
