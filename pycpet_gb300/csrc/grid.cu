@@ -405,7 +405,9 @@ constexpr int kFlagThreads = 512;
 constexpr int kFlagChunk = kFlagThreads * 8;  // points of a frame per flagging CTA
 constexpr int kMagBins = 4096;  // bits 30..19 of the float |E|^2: exponent + 4 mantissa bits
 constexpr int kBinsPerThread = kMagBins / kFlagThreads;
-constexpr int kRefineThreads = 1024;
+// 256 threads: the refinement CTAs must fit beside a serving engine launch
+// that holds half of every SM's registers (engine.cu), as the grid CTAs do.
+constexpr int kRefineThreads = 256;
 
 // Integer-only reads of doubles.  GB300's FP64 pipe is 1/64 of its FP32 pipe
 // and conversions from double run on it, so the refinement's helpers take a
@@ -838,7 +840,7 @@ cudaError_t launch_grid_refine(int n_frames, int64_t n_charges, int64_t max_poin
   grid_mag_hist_kernel<<<fgrid, kFlagThreads, 0, s>>>(desc, out, hist);
   const float tau2 = static_cast<float>(tau * tau);
   grid_flag_kernel<<<fgrid, kFlagThreads, 0, s>>>(desc, out, hist, tau2, list, count);
-  const int ctas = std::max(num_sms, 1) * 2;
+  const int ctas = std::max(num_sms, 1) * 8;
   if (clamp)
     grid_refine_kernel<true><<<ctas, kRefineThreads, 0, s>>>(desc, list, count, points, dfq, out);
   else

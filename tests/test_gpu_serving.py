@@ -159,3 +159,40 @@ def test_admission_retries_when_full(gpu_lib):
         np.testing.assert_array_equal(
             r.result, topo_lines(r.starts, r.n_iter, frames[0]["x"], frames[0]["q"], r.step, r.half_dims))
     srv.close()
+
+
+def test_grid_requests_run_beside_the_streamline_engine(gpu_lib):
+    """With the engine at one CTA per SM busy on a long streamline request,
+    volume (refined FP32C field), potential and point requests submitted after
+    it finish while the streamline request is still running: every kernel of
+    the grid path fits in the half of each SM the engine leaves free."""
+    import time
+
+    from pycpet_gb300.serving import Request, Server
+    from pycpet_gb300.synth import make_frame
+
+    srv = Server(precision="fp32c", line_capacity=100_000, charge_capacity=50_000, max_requests=64,
+                 engine_ctas_per_sm=1)
+    try:
+        fr = make_frame(20000, seed=71)
+        srv.add_frame(0, fr["x"], fr["q"])
+        rng = np.random.default_rng(72)
+        topo = Request("topo", 0, 0.0, starts=rng.uniform(-1.5, 1.5, (40_000, 3)), n_iter=6000, step=0.001)
+        g = np.linspace(-1.0, 1.0, 21)
+        pts = np.stack(np.meshgrid(g, g, g, indexing="ij"), -1).reshape(-1, 3)
+        grid = [Request(k, 0, 0.0, points=pts) for k in ("volume", "volume_esp")]
+        grid.append(Request("point_field", 0, 0.0, points=pts[:20]))
+        now = time.perf_counter()
+        for r in [topo] + grid:
+            r.arrival = now
+            assert srv.submit(r)
+        t_end = time.perf_counter() + 60
+        while any(r.status != "done" for r in grid) and time.perf_counter() < t_end:
+            srv.step()
+        assert all(r.status == "done" for r in grid)
+        assert topo.status == "running", "the grid requests waited for the streamline request"
+        while srv.busy() and time.perf_counter() < t_end:
+            srv.step()
+        assert topo.status == "done"
+    finally:
+        srv.close()
