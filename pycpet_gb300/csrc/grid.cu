@@ -670,79 +670,67 @@ __device__ __forceinline__ void df_add(float& h, float& l, float bh, float bl) {
   l = __fsub_rn(e, __fsub_rn(h, s));
 }
 
-// Recomputes the listed points in double-float arithmetic.  A CTA takes
-// kRefinePts consecutive list entries at a time (the flag kernel writes each
-// of its chunks' points contiguously, so they mostly share a frame); each run
-// of entries of one frame is evaluated together: the frame's charges
-// (double-float records, pack_df_kernel) are split over the threads and every
-// charge loaded once serves all points of the run.  Each point's arithmetic
-// and summation order are those of a run of one, so results do not depend on
-// how entries are grouped.  The threads' sums are combined by a fixed tree.
-constexpr int kRefinePts = 4;
-
+// Recomputes the listed points in double-float arithmetic: one CTA per point
+// at a time, the frame's charges (double-float records, pack_df_kernel) split
+// over the threads.  Each thread keeps two independent sums (its even and odd
+// charges), so two dependent double-float chains are in flight; the two are
+// added at the end and the threads' sums combined by a fixed tree.
 template <bool CLAMP>
 __global__ void __launch_bounds__(kRefineThreads)
     grid_refine_kernel(const int64_t* __restrict__ desc, const int64_t* __restrict__ list,
                        const int* __restrict__ count, const double* __restrict__ points,
                        const float4* __restrict__ dfq, double* __restrict__ out) {
-  __shared__ float red[kRefineThreads / 32][kRefinePts][6];
+  __shared__ float red[kRefineThreads / 32][6];
   const int n_list = *count;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  const int n_groups = (n_list + kRefinePts - 1) / kRefinePts;
-  for (int g = blockIdx.x; g < n_groups; g += gridDim.x) {
-    const int g0 = g * kRefinePts, g1 = min(n_list, g0 + kRefinePts);
-    for (int e0 = g0; e0 < g1;) {
-      const int64_t f = list[2 * e0 + 1];
-      int m = 1;  // entries of this run (same frame)
-      while (e0 + m < g1 && list[2 * (e0 + m) + 1] == f) ++m;
-      const int64_t co = desc[4 * f], n = desc[4 * f + 1];
-      float ph[kRefinePts][3], pl[kRefinePts][3];
-      float sh[kRefinePts][3], sl[kRefinePts][3];
+  for (int e = blockIdx.x; e < n_list; e += gridDim.x) {
+    const int64_t row = list[2 * e];
+    const int64_t f = list[2 * e + 1];
+    const int64_t co = desc[4 * f], n = desc[4 * f + 1];
+    float ph[3], pl[3];
 #pragma unroll
-      for (int t = 0; t < kRefinePts; ++t) {
-        const int64_t row = list[2 * (e0 + (t < m ? t : 0))];  // idle slots repeat slot 0
-#pragma unroll
-        for (int k = 0; k < 3; ++k) {
-          ph[t][k] = dbl_hi_float(points[3 * row + k]);
-          pl[t][k] = dbl_lo_float(points[3 * row + k]);
-          sh[t][k] = sl[t][k] = 0.f;
-        }
-      }
-      for (int64_t j = threadIdx.x; j < n; j += kRefineThreads) {
-        const float4 hi = dfq[2 * (co + j)], lo = dfq[2 * (co + j) + 1];
-#pragma unroll
-        for (int t = 0; t < kRefinePts; ++t)
-          if (t < m) df_field_term<CLAMP>(ph[t], pl[t], hi, lo, sh[t], sl[t]);
-      }
-#pragma unroll
-      for (int t = 0; t < kRefinePts; ++t) {
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1)
-#pragma unroll
-          for (int k = 0; k < 3; ++k) {
-            const float bh = __shfl_xor_sync(0xffffffffu, sh[t][k], o);
-            const float bl = __shfl_xor_sync(0xffffffffu, sl[t][k], o);
-            df_add(sh[t][k], sl[t][k], bh, bl);
-          }
-        if (lane == 0)
-#pragma unroll
-          for (int k = 0; k < 3; ++k) {
-            red[warp][t][2 * k] = sh[t][k];
-            red[warp][t][2 * k + 1] = sl[t][k];
-          }
-      }
-      __syncthreads();
-      if (threadIdx.x < 3 * m) {
-        const int t = threadIdx.x / 3, k = threadIdx.x % 3;
-        float h = red[0][t][2 * k], l = red[0][t][2 * k + 1];
-#pragma unroll
-        for (int w = 1; w < kRefineThreads / 32; ++w)
-          df_add(h, l, red[w][t][2 * k], red[w][t][2 * k + 1]);
-        out[3 * list[2 * (e0 + t)] + k] = (static_cast<double>(h) + static_cast<double>(l)) * kCoulomb;
-      }
-      __syncthreads();
-      e0 += m;
+    for (int k = 0; k < 3; ++k) {
+      ph[k] = dbl_hi_float(points[3 * row + k]);
+      pl[k] = dbl_lo_float(points[3 * row + k]);
     }
+    float sh[3] = {0.f, 0.f, 0.f}, sl[3] = {0.f, 0.f, 0.f};
+    float th[3] = {0.f, 0.f, 0.f}, tl[3] = {0.f, 0.f, 0.f};
+    int64_t j = threadIdx.x;
+    for (; j + kRefineThreads < n; j += 2 * kRefineThreads) {
+      const float4 hi0 = dfq[2 * (co + j)], lo0 = dfq[2 * (co + j) + 1];
+      const float4 hi1 = dfq[2 * (co + j + kRefineThreads)], lo1 = dfq[2 * (co + j + kRefineThreads) + 1];
+      df_field_term<CLAMP>(ph, pl, hi0, lo0, sh, sl);
+      df_field_term<CLAMP>(ph, pl, hi1, lo1, th, tl);
+    }
+    if (j < n) {
+      const float4 hi0 = dfq[2 * (co + j)], lo0 = dfq[2 * (co + j) + 1];
+      df_field_term<CLAMP>(ph, pl, hi0, lo0, sh, sl);
+    }
+#pragma unroll
+    for (int k = 0; k < 3; ++k) df_add(sh[k], sl[k], th[k], tl[k]);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1)
+#pragma unroll
+      for (int k = 0; k < 3; ++k) {
+        const float bh = __shfl_xor_sync(0xffffffffu, sh[k], o);
+        const float bl = __shfl_xor_sync(0xffffffffu, sl[k], o);
+        df_add(sh[k], sl[k], bh, bl);
+      }
+    if (lane == 0)
+#pragma unroll
+      for (int k = 0; k < 3; ++k) {
+        red[warp][2 * k] = sh[k];
+        red[warp][2 * k + 1] = sl[k];
+      }
+    __syncthreads();
+    if (threadIdx.x < 3) {
+      const int k = threadIdx.x;
+      float h = red[0][2 * k], l = red[0][2 * k + 1];
+#pragma unroll
+      for (int w = 1; w < kRefineThreads / 32; ++w) df_add(h, l, red[w][2 * k], red[w][2 * k + 1]);
+      out[3 * row + k] = (static_cast<double>(h) + static_cast<double>(l)) * kCoulomb;
+    }
+    __syncthreads();
   }
 }
 
