@@ -109,14 +109,19 @@ def _time_ms(run, reps: int) -> float:
 
 
 def tune_grid(frames, kind="field", precision="fp32c", reps=3, verbose=False):
-    """Times the grid variants on `frames` ((points, x, q) per frame); keeps the fastest."""
+    """Times the grid variants on `frames` ((points, x, q) per frame); keeps the
+    fastest.  Each variant is timed as a CUDA-graph plan replay, so the host's
+    planning of the work items (which grows with their number) stays out of the
+    device time being compared."""
     gb = GridBatch(frames, kind=kind, precision=precision, device=True)
     k = key(OP_GRID, precision, FIELD if kind == "field" else ESP, gb.pair_evals)
     n_var = lib().cpetgb_tune_variants(OP_GRID)
     times = []
     for v in range(n_var):
         set_variant(k, v)
-        times.append(_time_ms(gb.run, reps))
+        plan = GridBatch(frames, kind=kind, precision=precision, device=True, graph=True)
+        times.append(_time_ms(plan.run, reps))
+        del plan
     best = int(np.argmin(times))
     set_variant(k, best)
     if verbose:
