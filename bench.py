@@ -199,6 +199,8 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-extras", action="store_true", help="skip the FP64 / grid / CPU comparison legs")
     ap.add_argument("--lines", type=int, default=N_LINES, help="streamlines per step (smaller cases for ncu)")
+    ap.add_argument("--precision", default="fp32c", choices=["fp32c", "fp64"],
+                    help="topo workload: arithmetic form of the timed step (fp64: the plain drop-in form)")
     ap.add_argument("--workload", default="topo", choices=["topo", "grid", "topo-batch", "serve", "cluster", "topo-dipole", "dat", "prep"],
                     help="grid: the 64-frame batched volume + volume_ESP workload; topo-batch: "
                          "frames of 5,000-20,000 charges with uneven line counts in one launch")
@@ -259,14 +261,15 @@ def main():
     hist_range = ((0.0, 5.2), (0.0, None))
 
     # step counts (deterministic) for the pair-evaluation count
-    res, steps = topo_lines(d_starts, d_caps, d_x, d_q, STEP, [HALF] * 3, precision="fp32c", return_steps=True)
+    prec = args.precision
+    res, steps = topo_lines(d_starts, d_caps, d_x, d_q, STEP, [HALF] * 3, precision=prec, return_steps=True)
     torch.cuda.synchronize()
     pe_step = pair_evals(steps.cpu().numpy(), N_CHARGES)
 
     def step(ev_k0=None, ev_k1=None):
         if ev_k0 is not None:
             ev_k0.record(stream)
-        r = topo_lines(d_starts, d_caps, d_x, d_q, STEP, [HALF] * 3, precision="fp32c")
+        r = topo_lines(d_starts, d_caps, d_x, d_q, STEP, [HALF] * 3, precision=prec)
         if ev_k1 is not None:
             ev_k1.record(stream)
         return r, topo_hist2d(r, bins=(20, 20), range=hist_range)
@@ -277,6 +280,7 @@ def main():
     ffma_scalar, ffma2 = _lib.measure_peak(0), _lib.measure_peak(3)
     ffma = max(ffma_scalar, ffma2)
     loop_rate = _lib.measure_peak(4)  # the sweep's inner loop alone (pair evaluations/s)
+    peak = ffma if prec == "fp32c" else _lib.measure_peak(1)  # FP64 form: the DFMA pipe
     torch.cuda.synchronize()
 
     evs = [[torch.cuda.Event(enable_timing=True) for _ in range(4)] for _ in range(args.steps)]
@@ -321,17 +325,19 @@ def main():
         "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic (seeded; no dataset ships with the benchmark)",
         "config": dict(workload_config(), n_lines=n_lines),
-        "precision": "fp32c", "precision_detail": PRECISION_DETAIL,
+        "precision": prec, "precision_detail": PRECISION_DETAIL if prec == "fp32c" else "IEEE double throughout",
         "pair_evals_per_s": pe_per_s,
         "latency_ms": {"p50": float(np.percentile(step_ms, 50)), "p99": float(np.percentile(step_ms, 99))},
-        "roofline": {"bound": "fp32", "achieved": achieved / 1e12, "peak": ffma / 1e12, "unit": "TFLOP/s",
-                     "frac": achieved / ffma, "traffic": traffic,
+        "roofline": {"bound": "fp32" if prec == "fp32c" else "fp64", "achieved": achieved / 1e12,
+                     "peak": peak / 1e12, "unit": "TFLOP/s", "frac": achieved / peak,
+                     "traffic": traffic if prec == "fp32c" else None,
                      "traffic_note": "DRAM bytes per launch (ncu capture of 20,000 lines scaled by lines); "
                                      "the kernel is FP32-pipe bound, the charges stay in shared memory",
                      "frac_ceiling": 17 / 24,
                      "sweep_loop_pair_evals_per_s": loop_rate,
                      "frac_of_sweep_loop": (pe_step / avg_kern_s) / loop_rate,
-                     "kernel": "topo_kernel (FP32C, charges resident in shared memory)",
+                     "kernel": ("topo_kernel (FP32C, charges resident in shared memory)" if prec == "fp32c"
+                                else "topo_kernel (FP64, charges from L2)"),
                      "work": f"{FLOPS_PER_PAIR} flop per pair evaluation x sum_lines N*(max(s,2)+2)",
                      "peak_source": "FP32 pipe measured in this run (cpetgb_measure_peak): the higher of "
                                     f"FFMA {ffma_scalar / 1e12:.1f} and packed FFMA2 {ffma2 / 1e12:.1f} TFLOP/s; "
@@ -345,11 +351,11 @@ def main():
         # every one of the --steps repetitions timed
         pin = lambda a: torch.from_numpy(np.ascontiguousarray(a)).pin_memory().numpy()
         h_starts, h_caps, h_x, h_q = pin(starts), pin(caps), pin(x), pin(q)
-        topo_lines(h_starts[:1024], h_caps[:1024], h_x, h_q, STEP, [HALF] * 3, precision="fp32c")
+        topo_lines(h_starts[:1024], h_caps[:1024], h_x, h_q, STEP, [HALF] * 3, precision=prec)
         e2e_t = []
         for _ in range(args.steps):
             t0 = time.perf_counter()
-            r = topo_lines(h_starts, h_caps, h_x, h_q, STEP, [HALF] * 3, precision="fp32c")
+            r = topo_lines(h_starts, h_caps, h_x, h_q, STEP, [HALF] * 3, precision=prec)
             c = topo_hist2d(r, bins=(20, 20), range=hist_range)
             e2e_t.append(time.perf_counter() - t0)
         # in: starts, caps, charges; the histogram call uploads the (L,2) result again
