@@ -597,6 +597,11 @@ __device__ __forceinline__ void two_prod(float a, float b, float& p, float& e) {
   e = __fmaf_rn(a, b, -p);
 }
 
+// 1e-6 as a double-float pair: the float nearest to it and the float nearest
+// to the rest (1e-6 - 9.99999997e-7 = 2.5e-15).
+constexpr float kClampH = 1e-6f;
+constexpr float kClampL = static_cast<float>(1e-6 - static_cast<double>(1e-6f));
+
 // The field term of one charge at one point in double-float, added to
 // (sh[k], sl[k]).  Point (ph, pl), charge coordinates (ch, cl) and charge
 // (qh, ql) as float pairs.  Relative error of the term about 1e-13.
@@ -628,11 +633,11 @@ __device__ __forceinline__ void df_field_term(const float (&ph)[3], const float 
     r2l = __fsub_rn(r2l, __fsub_rn(h, r2h));
     r2h = h;
   }
-  if (CLAMP && r2h < 1.0001e-6f) {  // compute_looped_field's r^2 >= 1e-6
-    if (static_cast<double>(r2h) + static_cast<double>(r2l) < 1e-6) {
-      r2h = 1e-6f;
-      r2l = static_cast<float>(1e-6 - static_cast<double>(1e-6f));
-    }
+  // compute_looped_field's r^2 >= 1e-6, compared as double-float values
+  // (lexicographically: both pairs are normalised), FP32 operations only.
+  if (CLAMP && (r2h < kClampH || (r2h == kClampH && r2l < kClampL))) {
+    r2h = kClampH;
+    r2l = kClampL;
   }
   // r^-1: MUFU seed refined by one Newton step with the residual in double-float
   const float y0 = rsqrt_mufu(r2h);

@@ -374,7 +374,10 @@ __device__ __forceinline__ void sweep_f32x2(const ulonglong2* __restrict__ sA,
   total = h[0];
 }
 
-// FP64: charges from global memory (padded with zero charges far away).
+// FP64: charges from global memory (padded with zero charges far away).  Every
+// operation in double precision; r^-1 from the double rsqrt (1 ulp), whose few
+// FP64-pipe operations replace a correctly rounded sqrt and division (GB300's
+// FP64 pipe is 1/64 of its FP32 pipe).
 template <int NA, int S>
 __device__ __forceinline__ void sweep_f64(const Charge64* __restrict__ g, int n_pad, int lane,
                                           const double (&ex)[S][3], double (&E)[S][3]) {
@@ -392,8 +395,8 @@ __device__ __forceinline__ void sweep_f64(const Charge64* __restrict__ g, int n_
       const double dy = __dsub_rn(ex[e][1], ch.y);
       const double dz = __dsub_rn(ex[e][2], ch.z);
       const double r2 = __fma_rn(dx, dx, __fma_rn(dy, dy, __dmul_rn(dz, dz)));
-      const double r = sqrt(r2);
-      const double w = __ddiv_rn(ch.q, __dmul_rn(r2, r));
+      const double ri = rsqrt(r2);  // double-precision reciprocal square root (1 ulp)
+      const double w = __dmul_rn(ch.q, __dmul_rn(ri, __dmul_rn(ri, ri)));
       acc[e][0] = __fma_rn(w, dx, acc[e][0]);
       acc[e][1] = __fma_rn(w, dy, acc[e][1]);
       acc[e][2] = __fma_rn(w, dz, acc[e][2]);
@@ -411,7 +414,8 @@ __device__ __forceinline__ void sweep_f64(const Charge64* __restrict__ g, int n_
 }
 
 // FP64 dipoles: Dipole64 records read from global memory (L2), padded with
-// zero moments far away.  Same term as dipole_run, in IEEE double.
+// zero moments far away.  Same term as dipole_run, in double precision (r^-1
+// from the double rsqrt, as sweep_f64).
 template <int NA, int S>
 __device__ __forceinline__ void sweep_dipole_f64(const Dipole64* __restrict__ g, int n_pad, int lane,
                                                  const double (&ex)[S][3], double (&E)[S][3]) {
@@ -429,7 +433,9 @@ __device__ __forceinline__ void sweep_dipole_f64(const Dipole64* __restrict__ g,
       const double dy = __dsub_rn(ex[e][1], d.y);
       const double dz = __dsub_rn(ex[e][2], d.z);
       const double r2 = __fma_rn(dx, dx, __fma_rn(dy, dy, __dmul_rn(dz, dz)));
-      const double r5 = __ddiv_rn(1.0, __dmul_rn(__dmul_rn(r2, r2), sqrt(r2)));
+      const double ri = rsqrt(r2);  // double-precision reciprocal square root (1 ulp)
+      const double ri2 = __dmul_rn(ri, ri);
+      const double r5 = __dmul_rn(__dmul_rn(ri2, ri2), ri);
       const double dot = __fma_rn(3.0 * d.mx, dx, __fma_rn(d.my, dy, __dmul_rn(d.mz, dz)));
       acc[e][0] = __fma_rn(r5, __fma_rn(dot, dx, -__dmul_rn(d.mx, r2)), acc[e][0]);
       acc[e][1] = __fma_rn(r5, __fma_rn(dot, dy, -__dmul_rn(d.my, r2)), acc[e][1]);
