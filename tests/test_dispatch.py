@@ -7,7 +7,10 @@ self.Q, self.mesh, self.random_start_points, ...), the return shapes and
 dtypes the dispatcher's writers expect.  It runs where the reference checkout
 is present (CPETGB_REF, default /root/reference) and needs no GPU: the three
 device calls the methods make are replaced here by the FP64 test oracle.
-The same outputs from the GPU are checked in test_gpu_dispatch.py.
+It runs twice: with the dispatcher's own writers, and with
+patch_pycpet(gpu_writers=True) installing this package's save_numpy_as_dat and
+savetxt (their GPU text formatting replaced by numpy's here).  The same outputs
+from the GPU are checked in test_gpu_dispatch.py.
 """
 import os
 import sys
@@ -43,15 +46,36 @@ def test_reference_dispatcher_with_drop_in_methods(oracle, golden, monkeypatch, 
     monkeypatch.setattr(drop_in, "field_grid", field_grid)
     monkeypatch.setattr(drop_in, "esp_grid", esp_grid)
     monkeypatch.setattr(drop_in, "topo_lines", topo_lines)
+    # the text writers' GPU formatting, replaced by numpy's own (the bytes the
+    # GPU writers must produce) so the writer glue runs here too
+    import io
+
+    from pycpet_gb300 import calculator as C
+
+    def text(fmt):
+        def f(values):
+            sink = io.BytesIO()
+            np.savetxt(sink, np.asarray(values).reshape(len(values), -1), fmt=fmt)
+            return sink.getvalue()
+        return f
+
+    monkeypatch.setattr(C, "format_fixed3", text("%.3f"))
+    monkeypatch.setattr(C, "format_sci18", text("%.18e"))
+    from CPET.source import CPET as dispatcher
+
     cls = scalc.calculator
     saved = {n: cls.__dict__[n] for n in drop_in.HOT_METHODS if n in cls.__dict__}
+    saved_writers = (dispatcher.np, dispatcher.save_numpy_as_dat)
     try:
-        assert drop_in.patch_pycpet("fp64") is cls
         g = golden("ref_dispatch.npz")
-        for m in D.METHODS:
-            files = mg.run_dispatcher(m, os.path.join(REF, mg.DISPATCH_PDB), str(tmp_path / m))
-            D.compare(m, files, D.fixture_files(g, m))
+        for writers in (False, True):
+            assert drop_in.patch_pycpet("fp64", gpu_writers=writers) is cls
+            assert (dispatcher.save_numpy_as_dat is C.save_numpy_as_dat) == writers
+            for m in D.METHODS:
+                files = mg.run_dispatcher(m, os.path.join(REF, mg.DISPATCH_PDB), str(tmp_path / f"{m}{writers}"))
+                D.compare(m, files, D.fixture_files(g, m))
     finally:
+        dispatcher.np, dispatcher.save_numpy_as_dat = saved_writers
         for n in drop_in.HOT_METHODS:
             if n in saved:
                 setattr(cls, n, saved[n])
