@@ -331,17 +331,19 @@ def main():
         "roofline": {"bound": "fp32" if prec == "fp32c" else "fp64", "achieved": achieved / 1e12,
                      "peak": peak / 1e12, "unit": "TFLOP/s", "frac": achieved / peak,
                      "traffic": traffic if prec == "fp32c" else None,
-                     "traffic_note": "DRAM bytes per launch (ncu capture of 20,000 lines scaled by lines); "
-                                     "the kernel is FP32-pipe bound, the charges stay in shared memory",
+                     "traffic_note": ("DRAM bytes per launch (ncu capture of 20,000 lines scaled by lines); "
+                                      "the kernel is FP32-pipe bound, the charges stay in shared memory")
+                     if prec == "fp32c" else "FP64-pipe bound; charges read from L2",
                      "frac_ceiling": 17 / 24,
                      "sweep_loop_pair_evals_per_s": loop_rate,
                      "frac_of_sweep_loop": (pe_step / avg_kern_s) / loop_rate,
                      "kernel": ("topo_kernel (FP32C, charges resident in shared memory)" if prec == "fp32c"
                                 else "topo_kernel (FP64, charges from L2)"),
                      "work": f"{FLOPS_PER_PAIR} flop per pair evaluation x sum_lines N*(max(s,2)+2)",
-                     "peak_source": "FP32 pipe measured in this run (cpetgb_measure_peak): the higher of "
-                                    f"FFMA {ffma_scalar / 1e12:.1f} and packed FFMA2 {ffma2 / 1e12:.1f} TFLOP/s; "
-                                    "MEASURED_PEAKS.json holds HBM and bf16 figures only"},
+                     "peak_source": ("FP32 pipe measured in this run (cpetgb_measure_peak): the higher of "
+                                     f"FFMA {ffma_scalar / 1e12:.1f} and packed FFMA2 {ffma2 / 1e12:.1f} TFLOP/s"
+                                     if prec == "fp32c" else "DFMA throughput measured in this run")
+                                    + "; MEASURED_PEAKS.json holds HBM and bf16 figures only"},
         "gpu_launches": 4 * args.steps,
         "clocks": clocks,
     }
