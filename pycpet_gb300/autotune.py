@@ -22,7 +22,6 @@ import os
 
 import numpy as np
 
-from . import _lib
 from ._lib import ESP, FIELD, check, lib
 from .core import GridBatch, TopoBatch, precision_code
 

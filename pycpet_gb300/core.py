@@ -16,7 +16,6 @@ import math
 
 import numpy as np
 
-from . import _lib
 from ._lib import DEVICE, ESP, FIELD, FP32C, FP64, HOST, check, lib
 
 PRECISIONS = {"fp64": FP64, "fp32c": FP32C, FP64: FP64, FP32C: FP32C}

@@ -36,7 +36,6 @@ from dataclasses import dataclass, field
 
 import numpy as np
 
-from . import _lib
 from ._lib import DEVICE, EAGAIN, ESP, FIELD, check, lib
 from .core import precision_code
 

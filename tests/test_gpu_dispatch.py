@@ -6,7 +6,6 @@ CPET(options).run() (tests/golden/ref_dispatch.npz; comparison rules in
 dispatch_outputs.py)."""
 import types
 
-import numpy as np
 import pytest
 
 import dispatch_outputs as D

@@ -8,7 +8,6 @@ code and its C library compiled from source):
 The FP64 oracle must agree with the FP32 reference to FP32 rounding; the FP32
 restatement must agree with the reference library more tightly still.
 """
-import os
 
 import numpy as np
 import pytest
