@@ -95,16 +95,17 @@ def make_dipole_frame(n_dipoles: int, seed: int, sigma: float = 0.3):
     return {"x": fr["x"], "mu": mu, "seed": seed}
 
 
-def volume_batch_specs(n_frames: int, seed: int = 2024):
+def volume_batch_specs(n_frames: int, seed: int = 2024, frame_seed0: int = 5000):
     """Frame shapes of the batched volume workload: per frame (n_charges,
     half_width, frame_seed) with N ~ U[3,000, 40,000] and half-widths 0.5, 1.0
-    or 1.5 A (11^3, 21^3 or 31^3 points at 0.1 A)."""
+    or 1.5 A (11^3, 21^3 or 31^3 points at 0.1 A); frame f's charges come from
+    seed frame_seed0 + f."""
     rng = np.random.default_rng(seed)
     specs = []
     for f in range(n_frames):
         n = int(rng.integers(3000, 40001))
         half = float(rng.choice([0.5, 1.0, 1.5]))
-        specs.append((n, half, 5000 + f))
+        specs.append((n, half, frame_seed0 + f))
     return specs
 
 
@@ -114,11 +115,11 @@ def cube_points(half: float, step: float = 0.1):
     return np.stack(np.meshgrid(g, g, g, indexing="ij"), -1).reshape(-1, 3)
 
 
-def volume_batch_frames(n_frames: int, seed: int = 2024, only=None):
+def volume_batch_frames(n_frames: int, seed: int = 2024, only=None, frame_seed0: int = 5000):
     """[(points, x, q)] of the batched volume workload (volume_batch_specs);
     ``only`` restricts it to the listed frame indices."""
     out = []
-    for f, (n, half, fs) in enumerate(volume_batch_specs(n_frames, seed)):
+    for f, (n, half, fs) in enumerate(volume_batch_specs(n_frames, seed, frame_seed0)):
         if only is not None and f not in only:
             continue
         fr = make_frame(n, seed=fs)

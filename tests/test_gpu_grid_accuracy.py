@@ -115,3 +115,20 @@ def test_clamp_near_tiles(gpu_lib, oracle):
     rel = np.linalg.norm(E32 - ref, axis=1) / nb
     assert rel[~is_near].max() <= REL
     assert rel[is_near].max() <= 1e-2
+
+
+def test_field_fp32c_per_point_on_other_seeded_frames(gpu_lib, oracle):
+    """The same bound on frames the refinement threshold was not chosen on:
+    the batched volume workload's distribution drawn with another seed (16
+    frames, 3,000-40,000 charges, 11^3 / 21^3 / 31^3 grids)."""
+    from pycpet_gb300 import GridBatch
+    from pycpet_gb300.synth import volume_batch_frames
+
+    frames = volume_batch_frames(16, seed=777, frame_seed0=90_000)
+    gb = GridBatch(frames, kind="field", precision="fp32c")
+    outs = gb.split(gb.run())
+    worst = 0.0
+    for (pts, x, q), E in zip(frames, outs):
+        ref = oracle.field_grid_f64(pts, x, q, clamp=True)
+        worst = max(worst, float(_per_point_rel(E, ref).max()))
+    assert worst <= REL, worst
