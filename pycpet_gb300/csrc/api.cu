@@ -343,7 +343,10 @@ int grid_batch_impl(int kind, int prec, int mem, int clamp, int n_frames, const 
   CK(launch_grid_final(kind, static_cast<int>(plan.finals.size()), d_fin, partial, dout, s),
      "grid reduction launch");
   const double tau = g_refine_tau.load();
-  if (kind == CPETGB_FIELD && prec == CPETGB_FP32C && tau > 0.0 && tot_ch > 0) {
+  // A frame of one or two points never has a point below tau x its lower
+  // median, so launches of such frames only (point fields) skip the pass.
+  if (kind == CPETGB_FIELD && prec == CPETGB_FP32C && tau > 0.0 && tot_ch > 0 &&
+      max_frame_points(n_frames, desc) >= 3) {
     int64_t *d_desc = nullptr, *list = nullptr;
     int* count = nullptr;
     unsigned char* dfq = nullptr;
@@ -902,7 +905,8 @@ int grid_plan_impl(cpetgb_plan** out_plan, int kind, int prec, int clamp, int n_
     return cuda_fail(e, "plan allocation");
   }
   const double tau = g_refine_tau.load();
-  const bool refine = kind == CPETGB_FIELD && prec == CPETGB_FP32C && tau > 0.0 && tot_ch > 0;
+  const bool refine = kind == CPETGB_FIELD && prec == CPETGB_FP32C && tau > 0.0 && tot_ch > 0 &&
+                      max_frame_points(n_frames, desc) >= 3;
   int64_t *d_desc = nullptr, *list = nullptr;
   int* count = nullptr;
   unsigned char* dfq = nullptr;
