@@ -98,6 +98,31 @@ def test_argument_validation_new_entry_points(built):
     assert L.cpetgb_topo_dipole_lines(5, 0, 1, 1, x.ctypes.data, None, 0.1, c.ctypes.data, x.ctypes.data,
                                       x.ctypes.data, out.ctypes.data, None, None, None) == _lib.EINVAL
     assert L.cpetgb_engine_set_ctas_per_sm(None, 2) == _lib.EINVAL
+    assert L.cpetgb_format_sci18(0, 2, 0, v.ctypes.data, None, 0, ctypes.byref(length), None) == _lib.EINVAL
+    assert L.cpetgb_format_sci18(5, 2, 3, v.ctypes.data, None, 0, ctypes.byref(length), None) == _lib.EINVAL
+
+
+def test_settings_and_checks_validate_arguments(built):
+    """Process-wide settings and the wait-limit check refuse bad values before
+    any device work; the per-call precision variants refuse bad precisions."""
+    import numpy as np
+    from pycpet_gb300 import _lib
+
+    L = _lib.lib()
+    old = L.cpetgb_field_refinement()
+    assert 0.0 <= old <= 1.0
+    for bad in (-0.5, 1.5, float("nan"), float("inf")):
+        assert L.cpetgb_set_field_refinement(bad) == _lib.EINVAL
+        assert "refinement" in _lib.last_error()
+    assert L.cpetgb_field_refinement() == old
+    assert L.cpetgb_set_field_refinement(0.25) == _lib.OK and L.cpetgb_field_refinement() == 0.25
+    assert L.cpetgb_set_field_refinement(old) == _lib.OK
+    for bad in (0.0, -1.0, 2.5, float("nan")):
+        assert L.cpetgb_check_wait_limit(bad) == _lib.EINVAL
+    x0 = np.zeros((1, 3), np.float32)
+    E = np.zeros((1, 3), np.float32)
+    assert L.cpetgb_compute_looped_field_p(7, 1, 1, x0.ctypes.data, x0.ctypes.data, x0.ctypes.data,
+                                           E.ctypes.data) == _lib.EINVAL
 
 
 def test_tuning_table_round_trip(built):
